@@ -1,0 +1,355 @@
+"""Benchmark: SAT throughput in GB/s (input + output bytes) against the
+measured HBM copy bandwidth of one GB300.
+
+Headline workload (one step = one SAT over one synthetic image already in
+HBM): f32 -> f32 plain SAT of an 8192 x 8192 image, uniform [0,1) values.
+Inputs (256 MiB) and outputs (256 MiB) are each larger than the 129 MB L2, so
+no L2 flush is needed between steps.  The same line also reports the 8192^2
+u8 -> u32 SAT, the compensated f32 SAT (and its time ratio to plain), the
+4096^2 f64 SAT and the batched uneven-image case.
+
+`--impl reference` times the reference's CPU integral image instead
+(IntegralImageParallel, pengdada/SAT integralImage.h:129-146, as restated in
+oracle/ with OpenMP over every host core) on the same workload.
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU
+(no data exchange: images are independent), "scaling": "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GB = 1e9
+W_HEAD, H_HEAD = 8192, 8192
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _traffic_from_profiles(key: str):
+    """DRAM bytes per launch of the dominant kernel, from the committed ncu
+    summary (profiles/*.md lines of the form `traffic_bytes_per_launch[key]: N`)."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for fn in sorted(os.listdir(d)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(d, fn)) as f:
+            for line in f:
+                tag = f"traffic_bytes_per_launch[{key}]:"
+                if line.strip().startswith(tag):
+                    try:
+                        return int(float(line.split(":", 1)[1].strip().split()[0]))
+                    except ValueError:
+                        return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = os.path.join("/tmp", f"satgb_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons, n = [], [], set(), 0
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                n += 1
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": n}
+
+
+def _time_steps(fn, steps, warmup, stream, min_warm_s=1.0):
+    """W untimed warm-up steps (at least min_warm_s of work, so the clock
+    sampler sees the GPU under load), then exactly `steps` timed steps with
+    one CUDA event pair per step on `stream`.  Returns (total_ms, per_step_ms)."""
+    import torch
+    t0 = time.time()
+    i = 0
+    while i < warmup or time.time() - t0 < min_warm_s:
+        fn()
+        i += 1
+        if i % 50 == 0:
+            stream.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for k in range(steps):
+        ev[k][0].record(stream)
+        fn()
+        ev[k][1].record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    per = [a.elapsed_time(b) for a, b in ev]
+    return start.elapsed_time(end), per
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import sat_gb300
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    sat_gb300._lib.load()
+
+    peak, peak_kind = _peaks()
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234 + rank)
+
+    # ---- headline: f32 8192^2 plain -------------------------------------------
+    x = torch.rand((H_HEAD, W_HEAD), dtype=torch.float32, device=dev, generator=g)
+    y = torch.empty_like(x)
+    step_bytes = x.numel() * 8
+    sampler = ClockSampler(local)
+    if rank == 0:
+        sampler.start()
+    l0 = sat_gb300.launch_count()
+
+    def headline():
+        sat_gb300.sat(x, torch.float32, out=y)
+
+    # barrier + sync on both sides of the timed region, max over ranks
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    total_ms, per = _time_steps(headline, args.steps, args.warmup, stream)
+    launches = sat_gb300.launch_count() - l0
+    sat_gb300.stream_check()
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    clocks = sampler.stop() if rank == 0 else None
+    timed_launches = args.steps  # one launch per step
+    warm_launches = launches - timed_launches
+    value = world * args.steps * step_bytes / (total_ms / 1e3) / GB
+    avg_launch_ms = statistics.mean(per)
+    achieved = step_bytes / (avg_launch_ms / 1e3) / GB
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    sub = {}
+    # ---- u8 -> u32 8192^2 -------------------------------------------------------
+    xb = torch.randint(0, 256, (H_HEAD, W_HEAD), dtype=torch.uint8, device=dev, generator=g)
+    yb = torch.empty((H_HEAD, W_HEAD), dtype=torch.uint32, device=dev)
+    ms, per_b = _time_steps(lambda: sat_gb300.scanrow_brlt(xb, torch.uint32, out=yb), 50, 5, stream, 0.2)
+    bb = xb.numel() * 5
+    sub["u8_u32_8192"] = {"gbs": round(bb / (statistics.median(per_b) / 1e3) / GB, 1),
+                          "ms_median": round(statistics.median(per_b), 4)}
+    sub["u8_u32_8192"]["frac_of_peak"] = round(sub["u8_u32_8192"]["gbs"] / peak, 4)
+    # ---- compensated f32 8192^2 -------------------------------------------------
+    ms, per_c = _time_steps(lambda: sat_gb300.sat(x, torch.float32, mode="compensated", out=y), 50, 5, stream, 0.2)
+    ms, per_p = _time_steps(headline, 50, 5, stream, 0.2)
+    sub["f32_compensated_8192"] = {"gbs": round(step_bytes / (statistics.median(per_c) / 1e3) / GB, 1),
+                                   "ms_median": round(statistics.median(per_c), 4),
+                                   "time_ratio_vs_plain": round(statistics.median(per_c) / statistics.median(per_p), 3)}
+    # ---- f64 4096^2 ---------------------------------------------------------------
+    xd = torch.rand((4096, 4096), dtype=torch.float64, device=dev, generator=g)
+    yd = torch.empty_like(xd)
+    ms, per_d = _time_steps(lambda: sat_gb300.sat(xd, torch.float64, out=yd), 50, 5, stream, 0.2)
+    sub["f64_4096"] = {"gbs": round(xd.numel() * 16 / (statistics.median(per_d) / 1e3) / GB, 1),
+                       "ms_median": round(statistics.median(per_d), 4)}
+    sat_gb300.stream_check()
+    del xb, yb, xd, yd
+
+    # ---- e2e: the same headline SAT through the C ABI with host buffers ---------
+    hx = torch.empty((H_HEAD, W_HEAD), dtype=torch.float32, pin_memory=True)
+    hx.copy_(x.cpu())
+    hy = torch.empty((H_HEAD, W_HEAD), dtype=torch.float32, pin_memory=True)
+    dx = torch.empty_like(x)
+    dy = torch.empty_like(x)
+
+    def e2e_step():
+        dx.copy_(hx, non_blocking=True)
+        sat_gb300.sat(dx, torch.float32, out=dy)
+        hy.copy_(dy, non_blocking=True)
+
+    e2e_steps = max(3, min(args.steps, 20))
+    ms_e2e, per_e = _time_steps(e2e_step, e2e_steps, 2, stream, 0.0)
+    e2e = {"value": round(e2e_steps * step_bytes / (ms_e2e / 1e3) / GB, 2), "unit": "GB/s",
+           "h2d_bytes_per_step": int(hx.numel() * 4), "d2h_bytes_per_step": int(hy.numel() * 4)}
+    del hx, hy, dx, dy
+
+    # ---- CPU baseline: the reference's IntegralImageParallel (oracle port) -----
+    cpu = cpu_baseline(args.cpu_seconds)
+
+    out = {
+        "metric": "SAT GB/s (in+out bytes), f32 8192x8192 plain; % of measured HBM copy bandwidth in roofline.frac",
+        "value": round(value, 1),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: torch.rand uniform [0,1) f32 (seeded); inputs and outputs 256 MiB each, larger than L2, no flush",
+        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step (BASELINE configs[1])",
+                   "width": W_HEAD, "height": H_HEAD, "in_dtype": "f32", "out_dtype": "f32",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{world}"},
+        "e2e": e2e,
+        "gpu_launches": int(timed_launches),
+        "warmup_launches": int(warm_launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "traffic": _traffic_from_profiles("f32_f32_8192"),
+                     "algorithmic_bytes_per_launch": step_bytes,
+                     "kernel": "satgb::sat_tile_kernel<float,float,float,fwd>"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "sub_results": sub,
+    }
+    print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(seconds: float):
+    """The reference's CPU integral image (oracle restatement of
+    IntegralImageParallel, OpenMP over all host cores) on the headline
+    workload, repeated for about `seconds` of CPU time."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    n = os.cpu_count() or 1
+    a = O.gen("f32u", 1, (H_HEAD, W_HEAD))
+    O.sat_parallel(a, np.float32, nthreads=n)  # warm
+    t0 = time.time()
+    reps = 0
+    while True:
+        O.sat_parallel(a, np.float32, nthreads=n)
+        reps += 1
+        if time.time() - t0 >= seconds:
+            break
+    dt = (time.time() - t0) / reps
+    return {"value": round(a.size * 8 / dt / GB, 3), "unit": "GB/s", "cores": n, "kind": "port",
+            "sample": f"{reps} full 8192x8192 f32 SATs with IntegralImageParallel (row pass then column pass), {n} OpenMP threads"}
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU integral image on this host."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    n = os.cpu_count() or 1
+    a = O.gen("f32u", 1, (H_HEAD, W_HEAD))
+    for _ in range(args.warmup):
+        O.sat_parallel(a, np.float32, nthreads=n)
+    t0 = time.time()
+    for _ in range(args.steps):
+        O.sat_parallel(a, np.float32, nthreads=n)
+    dt = time.time() - t0
+    value = args.steps * a.size * 8 / dt / GB
+    out = {
+        "impl": "reference",
+        "metric": "SAT GB/s (in+out bytes), f32 8192x8192 plain; % of measured HBM copy bandwidth in roofline.frac",
+        "value": round(value, 3), "unit": "GB/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: splitmix64 uniform [0,1) f32 (seeded)",
+        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step (BASELINE configs[1])",
+                   "width": W_HEAD, "height": H_HEAD, "in_dtype": "f32", "out_dtype": "f32"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": n, "kind": "port",
+                         "sample": f"each step one full 8192x8192 f32 IntegralImageParallel (oracle restatement), {n} OpenMP threads"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        from sat_gb300 import build as B
+        B.build()
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,229 @@
+/*
+ * satgb.h -- C ABI of libsatgb.so, a GB300 (sm_103a) summed-area-table
+ * (integral image) library.
+ *
+ * A drop-in for the three algorithm entry points of pengdada/SAT
+ * (integralImage/*.cu).  In the reference each one is a host driver that
+ * launches two kernels on caller-visible device buffers:
+ *
+ *   ScanRow-BRLT  (BlockScan)      BlockScan::Test / blockScan x2   ScanRow-BRLT.cu:182-255, kernel :24-180
+ *   BRLT-ScanRow  (SerialScan)     SerielScan::Test / serielScan x2 BRLT-Scan.cu:192-266,    kernel :15-127
+ *   ScanRowColumn (IncreamentScan) IncrementScan::Test / ScanX,ScanY ScanRowColumn.cu:424-499, kernels :16-268
+ *
+ * Here each entry point computes the same result -- the inclusive 2-D prefix
+ * sum out(y,x) = sum_{j<=y, i<=x} in(j,i) of a row-major width x height image
+ * -- with ONE launch of a single-pass tiled kernel (decoupled look-back in both
+ * tile directions), reading every input element once and writing every output
+ * element once.
+ *
+ * Conventions (kept from the reference):
+ *   - buffers are caller-owned DEVICE pointers;
+ *   - pitches are in ELEMENTS of the buffer's own type (GpuData::DataPitch,
+ *     cudaLib.cuh:178-180), pitch >= width;
+ *   - dtype codes are the reference's DataType enum (integralImage.h:22-32);
+ *   - scan_type is the reference's SCAN enum (integralImage.h:34-37).
+ *     Kogge-Stone and Ladner-Fischer give identical integer results; for
+ *     floating point this library's summation tree is its own and floats are
+ *     judged against an FP64 oracle, so scan_type is validated and recorded
+ *     but does not change the arithmetic.
+ * Added over the reference (which reports no errors: CUDA_CHECK_ERROR is an
+ * empty macro, cudaLib.cuh:21-22): every call returns a satgb_status; calls
+ * are asynchronous on the given stream (a cudaStream_t passed as void*, NULL
+ * = legacy default stream); device-side failures (a look-back wait that
+ * exceeded its time limit) are reported by satgb_stream_check().
+ *
+ * Integer outputs wrap modulo 2^32 exactly like the reference's CPU integral
+ * image (IntegralImageSerial, integralImage.h:105-124).
+ *
+ * Scratch: the look-back status words live in a per-stream workspace that the
+ * library allocates on first use (and grows when a larger image arrives) and
+ * frees in satgb_release().  Calls on distinct streams may run concurrently;
+ * calls on one stream are ordered by the stream.
+ */
+#ifndef SATGB_H
+#define SATGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SATGB_VERSION 100 /* 1.0.0 */
+
+typedef enum {
+  SATGB_OK = 0,
+  SATGB_ERR_INVALID_ARG = 1,       /* null pointer, width/height <= 0, pitch < width, bad enum */
+  SATGB_ERR_UNSUPPORTED_TYPES = 2, /* dtype pair (or mode) not offered */
+  SATGB_ERR_MISALIGNED = 3,        /* pointer not aligned to its element size */
+  SATGB_ERR_OVERFLOW = 4,          /* sizes whose byte extent does not fit in int64 */
+  SATGB_ERR_ALLOC = 5,             /* workspace allocation failed */
+  SATGB_ERR_CUDA = 6,              /* a CUDA runtime call failed (see satgb_last_error_string) */
+  SATGB_ERR_TIMEOUT = 7,           /* a device-side look-back wait exceeded its limit */
+  SATGB_ERR_NOT_FOUND = 8          /* no such plan / symbol / tuning entry */
+} satgb_status;
+
+/* The reference's DataType enum, integralImage.h:22-32.  u16/i16 are listed
+ * there but never dispatched; they are rejected here too. */
+typedef enum {
+  SATGB_U8 = 0,
+  SATGB_I8 = 1,
+  SATGB_U16 = 2,
+  SATGB_I16 = 3,
+  SATGB_U32 = 4,
+  SATGB_I32 = 5,
+  SATGB_F32 = 6,
+  SATGB_F64 = 7
+} satgb_dtype;
+
+/* The reference's SCAN enum, integralImage.h:34-37. */
+typedef enum { SATGB_SCAN_KOGGE_STONE = 0, SATGB_SCAN_LF = 1 } satgb_scan_type;
+
+typedef enum {
+  SATGB_MODE_PLAIN = 0,       /* arithmetic in the output type */
+  SATGB_MODE_COMPENSATED = 1  /* f32 outputs only: two-sum compensated carries */
+} satgb_mode;
+
+typedef enum {
+  SATGB_FORWARD = 0, /* out(y,x) = sum_{j<=y, i<=x} in(j,i)   (the SAT) */
+  SATGB_REVERSE = 1  /* out(y,x) = sum_{j>=y, i>=x} in(j,i)   (suffix SAT; the SAT's adjoint) */
+} satgb_direction;
+
+typedef void* satgb_stream; /* a cudaStream_t */
+
+/* ------------------------------------------------------------------------- */
+/* The three drop-in entry points.                                            */
+/* Type pairs (in_t -> out_t), as dispatched by the reference's host drivers  */
+/* (ScanRow-BRLT.cu:274-376, BRLT-Scan.cu:287-390, ScanRowColumn.cu:518-621): */
+/*   u8 -> u32, f32, f64      i8 -> i32, f32, f64      i32 -> i32, f64        */
+/*   f32 -> f32, f64          f64 -> f64                                      */
+/* plus u32 -> u32 (the reference's TDst -> TDst second-pass instantiation).  */
+/* ------------------------------------------------------------------------- */
+
+/* Replaces BlockScan::Test<TSrc,TDst,SCAN_TYPE> (ScanRow-BRLT.cu:182-255):
+ * its two blockScan launches (:225-226) over devA -> devTmp -> devB. */
+satgb_status satgb_scanrow_brlt(satgb_dtype in_t, satgb_dtype out_t, int scan_type,
+                                const void* d_in, int64_t in_pitch,
+                                void* d_out, int64_t out_pitch,
+                                int64_t width, int64_t height, satgb_stream stream);
+
+/* Replaces SerielScan::Test<TSrc,TDst,SCAN_TYPE> (BRLT-Scan.cu:192-266):
+ * its two serielScan launches (:237-238). */
+satgb_status satgb_brlt_scanrow(satgb_dtype in_t, satgb_dtype out_t, int scan_type,
+                                const void* d_in, int64_t in_pitch,
+                                void* d_out, int64_t out_pitch,
+                                int64_t width, int64_t height, satgb_stream stream);
+
+/* Replaces IncrementScan::Test<TSrc,TDst,SCAN_TYPE> (ScanRowColumn.cu:424-499):
+ * its ScanX + ScanY launches (:475-476). */
+satgb_status satgb_scanrowcolumn(satgb_dtype in_t, satgb_dtype out_t, int scan_type,
+                                 const void* d_in, int64_t in_pitch,
+                                 void* d_out, int64_t out_pitch,
+                                 int64_t width, int64_t height, satgb_stream stream);
+
+/* ------------------------------------------------------------------------- */
+/* Extended single-image call: compensated f32 and the reverse (suffix) SAT.  */
+/* No reference counterpart (the reference has neither).                      */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  satgb_dtype in_t, out_t;
+  int mode;      /* satgb_mode */
+  int direction; /* satgb_direction */
+  const void* d_in;
+  int64_t in_pitch;
+  void* d_out;
+  int64_t out_pitch;
+  int64_t width, height;
+} satgb_sat_desc;
+
+satgb_status satgb_sat_ex(const satgb_sat_desc* desc, satgb_stream stream);
+
+/* ------------------------------------------------------------------------- */
+/* Batched SAT: many images of uneven sizes, one persistent launch.           */
+/* No reference counterpart (the reference's drivers handle one image).       */
+/* A plan copies the image table to the device, picks a tile configuration    */
+/* (from the autotuner's cache when an entry exists) and captures the launch  */
+/* in a CUDA graph; exec replays the graph on `stream`.  All images share one */
+/* dtype pair, mode and direction.                                            */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  const void* d_in;
+  int64_t in_pitch;
+  void* d_out;
+  int64_t out_pitch;
+  int64_t width, height;
+} satgb_image;
+
+typedef struct satgb_batch_plan_s satgb_batch_plan;
+
+satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, satgb_dtype out_t,
+                                     int mode, int direction, const satgb_image* images,
+                                     int64_t n_images, satgb_stream stream);
+satgb_status satgb_batch_plan_exec(satgb_batch_plan* plan, satgb_stream stream);
+/* Launch without the graph (same kernel, same arguments). */
+satgb_status satgb_batch_plan_launch(satgb_batch_plan* plan, satgb_stream stream);
+satgb_status satgb_batch_plan_destroy(satgb_batch_plan* plan);
+/* Tiles in the plan and the configuration index it uses. */
+satgb_status satgb_batch_plan_info(const satgb_batch_plan* plan, int64_t* n_tiles, int* config);
+/* Synchronises `stream` and reports (and clears) a device-side error of the
+ * plan's launches, like satgb_stream_check does for single-image calls. */
+satgb_status satgb_batch_plan_check(satgb_batch_plan* plan, satgb_stream stream);
+
+/* ------------------------------------------------------------------------- */
+/* Autotuner: times each tile configuration on the given buffers (which are   */
+/* overwritten) and records the fastest for this dtype pair / mode / size     */
+/* bucket / SM count.  Entries persist in the JSON file named by              */
+/* SATGB_TUNE_CACHE when that variable is set.  best_config may be NULL.      */
+/* ------------------------------------------------------------------------- */
+satgb_status satgb_autotune(satgb_dtype in_t, satgb_dtype out_t, int mode,
+                            const void* d_in, int64_t in_pitch, void* d_out, int64_t out_pitch,
+                            int64_t width, int64_t height, satgb_stream stream, int* best_config);
+/* Number of tile configurations and a printable name for one. */
+int satgb_num_configs(void);
+const char* satgb_config_name(int config);
+/* Force a configuration for subsequent single-image calls (-1 = automatic). */
+satgb_status satgb_set_config(int config);
+
+/* ------------------------------------------------------------------------- */
+/* Errors, workspace, diagnostics.                                            */
+/* ------------------------------------------------------------------------- */
+
+/* Synchronises `stream`, then reports (and clears) a device-side error of the
+ * last calls on it: SATGB_ERR_TIMEOUT when a look-back wait gave up. */
+satgb_status satgb_stream_check(satgb_stream stream);
+
+/* Message for the last failing call on this host thread ("" when none). */
+const char* satgb_last_error_string(void);
+
+/* Frees every cached workspace (all streams); safe to call at any time when no
+ * call is in flight. */
+satgb_status satgb_release(void);
+
+/* Pre-sizes the workspace of `stream` for images up to width x height, so that
+ * a later call does not allocate (e.g. inside CUDA stream capture). */
+satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream);
+
+/* Allocation hook for the workspace (NULL restores cudaMalloc/cudaFree). */
+typedef void* (*satgb_alloc_fn)(size_t bytes, void* ctx);
+typedef void (*satgb_free_fn)(void* ptr, void* ctx);
+satgb_status satgb_set_allocator(satgb_alloc_fn alloc_fn, satgb_free_fn free_fn, void* ctx);
+
+/* Time limit of one look-back wait, in microseconds (default 2,000,000). */
+satgb_status satgb_set_wait_limit_us(int64_t us);
+
+/* Number of kernel launches this library has issued (all streams) since load:
+ * lets a caller count the library's launches inside a timed region. */
+int64_t satgb_launch_count(void);
+
+/* Test hook: the tile with this global index never publishes its look-back
+ * status, so the tiles that depend on it run into the wait limit and the call
+ * reports SATGB_ERR_TIMEOUT.  -1 (the default) disables it. */
+satgb_status satgb_debug_stall_tile(int64_t tile);
+
+int satgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SATGB_H */

@@ -1,0 +1,226 @@
+"""Torch-facing host API over the C ABI.
+
+The reference's operator interface is its three host drivers
+``BlockScan::Test``, ``SerielScan::Test`` and ``IncrementScan::Test``
+(pengdada/SAT integralImage/ScanRow-BRLT.cu:182-255, BRLT-Scan.cu:192-266,
+ScanRowColumn.cu:424-499), each templated over <TSrc, TDst, SCAN_TYPE> and
+computing the SAT of a row-major W x H image into a caller-visible device
+buffer.  The functions here keep those three names (``scanrow_brlt``,
+``brlt_scanrow``, ``scanrowcolumn``), the same type pairs and the same scan
+type argument, over torch CUDA tensors (device memory and streams only; the
+arithmetic is the CUDA kernel's).
+
+Images are 2-D tensors (height, width) whose rows are contiguous; the row
+stride becomes the pitch in elements, as in the reference's GpuData
+(cudaLib.cuh:178-180).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import torch
+
+from . import _lib
+from ._lib import (F32, F64, FORWARD, I8, I32, KOGGE_STONE_SCAN, LF_SCAN, MODE_COMPENSATED,
+                   MODE_PLAIN, REVERSE, U8, U32, SatError, check)
+
+_TORCH_TO_CODE = {
+    torch.uint8: U8,
+    torch.int8: I8,
+    torch.uint32: U32,
+    torch.int32: I32,
+    torch.float32: F32,
+    torch.float64: F64,
+}
+_CODE_TO_TORCH = {v: k for k, v in _TORCH_TO_CODE.items()}
+
+# default output type per input type (the reference's usual pairs)
+DEFAULT_OUT = {torch.uint8: torch.uint32, torch.int8: torch.int32, torch.uint32: torch.uint32,
+               torch.int32: torch.int32, torch.float32: torch.float32, torch.float64: torch.float64}
+
+# The pairs the reference's host drivers dispatch (ScanRow-BRLT.cu:274-376)
+# plus u32 -> u32.
+PAIRS = [
+    (torch.uint8, torch.uint32), (torch.uint8, torch.float32), (torch.uint8, torch.float64),
+    (torch.int8, torch.int32), (torch.int8, torch.float32), (torch.int8, torch.float64),
+    (torch.int32, torch.int32), (torch.int32, torch.float64),
+    (torch.uint32, torch.uint32),
+    (torch.float32, torch.float32), (torch.float32, torch.float64),
+    (torch.float64, torch.float64),
+]
+
+_MODES = {"plain": MODE_PLAIN, "compensated": MODE_COMPENSATED}
+
+
+def dtype_code(dt: torch.dtype) -> int:
+    try:
+        return _TORCH_TO_CODE[dt]
+    except KeyError:
+        raise SatError(_lib.ERR_UNSUPPORTED_TYPES, f"dtype {dt} has no satgb_dtype code") from None
+
+
+def _stream_handle(stream) -> int:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream) if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def _image_args(t: torch.Tensor):
+    if t.dim() != 2:
+        raise SatError(_lib.ERR_INVALID_ARG, f"an image is a 2-D tensor, got shape {tuple(t.shape)}")
+    h, w = t.shape
+    if w > 1 and t.stride(1) != 1:
+        raise SatError(_lib.ERR_INVALID_ARG, "image rows must be contiguous (stride(1) == 1)")
+    pitch = t.stride(0) if h > 1 else max(w, t.stride(0))
+    return t.data_ptr(), int(pitch), int(w), int(h)
+
+
+def _check_cuda(*ts: torch.Tensor) -> None:
+    for t in ts:
+        if not t.is_cuda:
+            raise SatError(_lib.ERR_INVALID_ARG, "tensors must be CUDA tensors (there is no CPU path)")
+
+
+def _prep_out(src: torch.Tensor, out_dtype, out: Optional[torch.Tensor]) -> torch.Tensor:
+    if out_dtype is None:
+        out_dtype = out.dtype if out is not None else DEFAULT_OUT.get(src.dtype, src.dtype)
+    if out is None:
+        out = torch.empty(src.shape, dtype=out_dtype, device=src.device)
+    elif out.dtype != out_dtype or out.shape != src.shape:
+        raise SatError(_lib.ERR_INVALID_ARG, "out has the wrong dtype or shape")
+    return out
+
+
+def _three(fn_name: str, src: torch.Tensor, out_dtype, scan_type: int, out, stream) -> torch.Tensor:
+    _check_cuda(src)
+    out = _prep_out(src, out_dtype, out)
+    _check_cuda(out)
+    ip, ipitch, w, h = _image_args(src)
+    op, opitch, _, _ = _image_args(out)
+    L = _lib.load()
+    check(getattr(L, fn_name)(dtype_code(src.dtype), dtype_code(out.dtype), int(scan_type), ip, ipitch,
+                              op, opitch, w, h, _stream_handle(stream)))
+    return out
+
+
+def scanrow_brlt(src: torch.Tensor, out_dtype=None, scan_type: int = LF_SCAN, out=None, stream=None):
+    """ScanRow-BRLT (BlockScan): SAT of `src` (BlockScan::Test, ScanRow-BRLT.cu:182-255)."""
+    return _three("satgb_scanrow_brlt", src, out_dtype, scan_type, out, stream)
+
+
+def brlt_scanrow(src: torch.Tensor, out_dtype=None, scan_type: int = LF_SCAN, out=None, stream=None):
+    """BRLT-ScanRow (SerialScan): SAT of `src` (SerielScan::Test, BRLT-Scan.cu:192-266)."""
+    return _three("satgb_brlt_scanrow", src, out_dtype, scan_type, out, stream)
+
+
+def scanrowcolumn(src: torch.Tensor, out_dtype=None, scan_type: int = LF_SCAN, out=None, stream=None):
+    """ScanRowColumn (IncreamentScan): SAT of `src` (IncrementScan::Test, ScanRowColumn.cu:424-499)."""
+    return _three("satgb_scanrowcolumn", src, out_dtype, scan_type, out, stream)
+
+
+ALGORITHMS = {
+    "ScanRow-BRLT": scanrow_brlt,
+    "BRLT-ScanRow": brlt_scanrow,
+    "ScanRowColumn": scanrowcolumn,
+}
+
+
+def sat(src: torch.Tensor, out_dtype=None, mode: str = "plain", reverse: bool = False, out=None,
+        stream=None) -> torch.Tensor:
+    """SAT (or, with reverse=True, the suffix SAT) of a 2-D image; mode
+    "compensated" carries two-sum error terms (f32 outputs)."""
+    _check_cuda(src)
+    out = _prep_out(src, out_dtype, out)
+    _check_cuda(out)
+    ip, ipitch, w, h = _image_args(src)
+    op, opitch, _, _ = _image_args(out)
+    d = _lib.satgb_sat_desc(dtype_code(src.dtype), dtype_code(out.dtype), _MODES[mode],
+                            REVERSE if reverse else FORWARD, ip, ipitch, op, opitch, w, h)
+    check(_lib.load().satgb_sat_ex(ctypes.byref(d), _stream_handle(stream)))
+    return out
+
+
+def stream_check(stream=None) -> None:
+    """Synchronises the stream and raises SatError(SATGB_ERR_TIMEOUT) when a
+    look-back wait of an earlier call gave up."""
+    check(_lib.load().satgb_stream_check(_stream_handle(stream)))
+
+
+def autotune(src: torch.Tensor, out: torch.Tensor, mode: str = "plain", stream=None) -> int:
+    """Times every tile configuration on (src, out) and records the best."""
+    _check_cuda(src, out)
+    ip, ipitch, w, h = _image_args(src)
+    op, opitch, _, _ = _image_args(out)
+    best = ctypes.c_int(-1)
+    check(_lib.load().satgb_autotune(dtype_code(src.dtype), dtype_code(out.dtype), _MODES[mode], ip, ipitch,
+                                     op, opitch, w, h, _stream_handle(stream), ctypes.byref(best)))
+    return best.value
+
+
+def set_config(config: int) -> None:
+    check(_lib.load().satgb_set_config(int(config)))
+
+
+def config_names() -> list:
+    L = _lib.load()
+    return [L.satgb_config_name(i).decode() for i in range(L.satgb_num_configs())]
+
+
+def set_wait_limit_us(us: int) -> None:
+    check(_lib.load().satgb_set_wait_limit_us(int(us)))
+
+
+def release() -> None:
+    check(_lib.load().satgb_release())
+
+
+class BatchPlan:
+    """Many images of uneven sizes in one persistent launch captured in a CUDA
+    graph (satgb_batch_plan_*).  The tensors must stay alive while the plan is
+    used; ``exec()`` replays the graph, ``launch()`` launches directly."""
+
+    def __init__(self, inputs: Sequence[torch.Tensor], outputs: Sequence[torch.Tensor],
+                 mode: str = "plain", reverse: bool = False, stream=None):
+        if len(inputs) != len(outputs) or not inputs:
+            raise SatError(_lib.ERR_INVALID_ARG, "inputs and outputs must be equal-length, non-empty lists")
+        in_dt, out_dt = inputs[0].dtype, outputs[0].dtype
+        arr = (_lib.satgb_image * len(inputs))()
+        for i, (a, b) in enumerate(zip(inputs, outputs)):
+            _check_cuda(a, b)
+            if a.dtype != in_dt or b.dtype != out_dt or a.shape != b.shape:
+                raise SatError(_lib.ERR_INVALID_ARG, f"image {i}: mixed dtypes or shape mismatch")
+            ip, ipitch, w, h = _image_args(a)
+            op, opitch, _, _ = _image_args(b)
+            arr[i] = _lib.satgb_image(ip, ipitch, op, opitch, w, h)
+        self._keep = (list(inputs), list(outputs))
+        self._plan = ctypes.c_void_p()
+        check(_lib.load().satgb_batch_plan_create(ctypes.byref(self._plan), dtype_code(in_dt), dtype_code(out_dt),
+                                                  _MODES[mode], REVERSE if reverse else FORWARD, arr,
+                                                  len(inputs), _stream_handle(stream)))
+
+    def exec(self, stream=None) -> None:
+        check(_lib.load().satgb_batch_plan_exec(self._plan, _stream_handle(stream)))
+
+    def launch(self, stream=None) -> None:
+        check(_lib.load().satgb_batch_plan_launch(self._plan, _stream_handle(stream)))
+
+    def check(self, stream=None) -> None:
+        check(_lib.load().satgb_batch_plan_check(self._plan, _stream_handle(stream)))
+
+    def info(self):
+        n = ctypes.c_int64()
+        c = ctypes.c_int()
+        check(_lib.load().satgb_batch_plan_info(self._plan, ctypes.byref(n), ctypes.byref(c)))
+        return {"n_tiles": n.value, "config": c.value}
+
+    def close(self) -> None:
+        if self._plan:
+            _lib.load().satgb_batch_plan_destroy(self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,745 @@
+// satgb_api.cu -- host side of libsatgb.so: the C ABI declared in
+// include/satgb.h.  Argument validation, the per-stream look-back workspace,
+// kernel-variant dispatch, the autotuner, batch plans (one persistent launch
+// captured in a CUDA graph) and device-error reporting.
+//
+// No CPU fallback exists: every SAT is computed by sat_tile_kernel.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/satgb.h"
+#include "sat_kernel.cuh"
+#include "sat_registry.h"
+
+namespace satgb {
+
+const TileConfig kConfigs[kNumConfigs] = {
+    {8, "tile64x(32*cpt) rpw8"},
+    {16, "tile128x(32*cpt) rpw16"},
+    {4, "tile32x(32*cpt) rpw4"},
+};
+
+const Variant* find_variant(int in_t, int out_t, int mode, int dir, int cfg) {
+  using ListFn = const Variant* (*)(int*);
+  static const ListFn lists[] = {variants_u8, variants_i8, variants_int32, variants_f32, variants_f64};
+  for (ListFn f : lists) {
+    int n = 0;
+    const Variant* v = f(&n);
+    for (int i = 0; i < n; ++i)
+      if (v[i].in_t == in_t && v[i].out_t == out_t && v[i].mode == mode && v[i].dir == dir && v[i].cfg == cfg)
+        return &v[i];
+  }
+  return nullptr;
+}
+
+}  // namespace satgb
+
+using namespace satgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::mutex g_mu;                      // guards every map below
+std::atomic<long long> g_launches{0}; // kernel launches issued
+std::atomic<long long> g_wait_limit_ns{2000000000LL};
+std::atomic<long long> g_stall_tile{-1};
+int g_forced_config = -1;
+satgb_alloc_fn g_alloc = nullptr;
+satgb_free_fn g_free = nullptr;
+void* g_alloc_ctx = nullptr;
+
+satgb_status fail(satgb_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return st;
+}
+
+satgb_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(SATGB_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+void* ws_alloc(size_t bytes) {
+  if (g_alloc) return g_alloc(bytes, g_alloc_ctx);
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void ws_free(void* p) {
+  if (!p) return;
+  if (g_free) g_free(p, g_alloc_ctx);
+  else cudaFree(p);
+}
+
+size_t dtype_size(int t) {
+  switch (t) {
+    case SATGB_U8:
+    case SATGB_I8: return 1;
+    case SATGB_U16:
+    case SATGB_I16: return 2;
+    case SATGB_U32:
+    case SATGB_I32:
+    case SATGB_F32: return 4;
+    case SATGB_F64: return 8;
+    default: return 0;
+  }
+}
+
+const char* dtype_name(int t) {
+  static const char* names[] = {"u8", "i8", "u16", "i16", "u32", "i32", "f32", "f64"};
+  return (t >= 0 && t < 8) ? names[t] : "?";
+}
+
+// One look-back workspace: a header block followed by the three status arrays.
+struct Workspace {
+  void* base = nullptr;
+  size_t bytes = 0;
+};
+
+struct Layout {
+  size_t row_off, col_off, corner_off, total;
+};
+
+Layout layout_for(long long n_tiles, const Variant* v) {
+  Layout L;
+  const size_t w = sizeof(unsigned long long);
+  L.row_off = sizeof(WsHeader);
+  L.col_off = L.row_off + (size_t)n_tiles * v->TH * v->K * w;
+  L.corner_off = L.col_off + (size_t)n_tiles * v->TW * v->K * w;
+  L.total = L.corner_off + (size_t)n_tiles * v->K * w;
+  return L;
+}
+
+// Workspaces of single-image calls, one per (device, stream).
+std::map<std::pair<int, void*>, Workspace> g_ws;
+
+satgb_status get_device(int* dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  return SATGB_OK;
+}
+
+// Makes sure ws holds at least `bytes`; called with g_mu held.
+satgb_status ensure_ws(Workspace& ws, size_t bytes, cudaStream_t s) {
+  if (ws.bytes >= bytes) return SATGB_OK;
+  bytes = std::max(bytes, ws.bytes + ws.bytes / 2);
+  bytes = (bytes + 4095) & ~(size_t)4095;
+  if (ws.base) {
+    cudaError_t e = cudaStreamSynchronize(s); // earlier calls may still use it
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    ws_free(ws.base);
+    ws.base = nullptr;
+    ws.bytes = 0;
+  }
+  void* p = ws_alloc(bytes);
+  if (!p) return fail(SATGB_ERR_ALLOC, "workspace allocation of %zu bytes failed", bytes);
+  cudaError_t e = cudaMemsetAsync(p, 0, bytes, s);
+  if (e != cudaSuccess) {
+    ws_free(p);
+    return cuda_fail(e, "cudaMemsetAsync");
+  }
+  ws.base = p;
+  ws.bytes = bytes;
+  return SATGB_OK;
+}
+
+struct DevInfo {
+  int sms = 0;
+};
+std::map<int, DevInfo> g_dev;
+std::map<std::pair<int, const void*>, int> g_occ; // (device, kernel) -> CTAs per SM
+
+satgb_status grid_for(int dev, const Variant* v, long long n_tiles, int* grid) {
+  auto it = g_dev.find(dev);
+  if (it == g_dev.end()) {
+    DevInfo d;
+    cudaError_t e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    it = g_dev.emplace(dev, d).first;
+  }
+  auto key = std::make_pair(dev, v->kernel);
+  auto jt = g_occ.find(key);
+  if (jt == g_occ.end()) {
+    int occ = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v->kernel, v->threads, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (occ < 1) occ = 1;
+    jt = g_occ.emplace(key, occ).first;
+  }
+  long long g = (long long)it->second.sms * jt->second;
+  *grid = (int)std::max(1LL, std::min(g, n_tiles));
+  return SATGB_OK;
+}
+
+bool pair_offered(int in_t, int out_t, int mode) {
+  // satgb_scanrow_brlt & co. offer the reference's dispatched pairs.
+  for (int cfg = 0; cfg < kNumConfigs; ++cfg)
+    if (find_variant(in_t, out_t, mode, 0, cfg)) return true;
+  return false;
+}
+
+struct ImgCheck {
+  const void* in;
+  void* out;
+  long long in_pitch, out_pitch, width, height;
+};
+
+satgb_status validate_image(const ImgCheck& c, size_t in_sz, size_t out_sz) {
+  if (c.width < 0 || c.height < 0) return fail(SATGB_ERR_INVALID_ARG, "negative width/height (%lld x %lld)", c.width, c.height);
+  if (c.width == 0 || c.height == 0) return SATGB_OK; // empty image: nothing to do
+  if (!c.in || !c.out) return fail(SATGB_ERR_INVALID_ARG, "null buffer");
+  if (c.in_pitch < c.width || c.out_pitch < c.width)
+    return fail(SATGB_ERR_INVALID_ARG, "pitch (%lld in, %lld out elements) smaller than width %lld", c.in_pitch, c.out_pitch, c.width);
+  if (((uintptr_t)c.in % in_sz) != 0 || ((uintptr_t)c.out % out_sz) != 0)
+    return fail(SATGB_ERR_MISALIGNED, "buffer not aligned to its element size");
+  // (height-1)*pitch + width elements must fit in int64 bytes
+  const long long lim = INT64_MAX / 16;
+  if (c.height > lim / std::max(1LL, c.in_pitch) || c.height > lim / std::max(1LL, c.out_pitch))
+    return fail(SATGB_ERR_OVERFLOW, "image extent overflows 64-bit byte offsets");
+  // the input and output must be the same buffer or disjoint
+  const char* ib = (const char*)c.in;
+  const char* ie = ib + ((c.height - 1) * c.in_pitch + c.width) * (long long)in_sz;
+  const char* ob = (const char*)c.out;
+  const char* oe = ob + ((c.height - 1) * c.out_pitch + c.width) * (long long)out_sz;
+  const bool same = ib == ob && in_sz == out_sz && c.in_pitch == c.out_pitch;
+  if (!same && ib < oe && ob < ie) return fail(SATGB_ERR_INVALID_ARG, "input and output overlap without being the same buffer");
+  return SATGB_OK;
+}
+
+ImageDesc make_desc(const ImgCheck& c, const Variant* v, size_t in_sz, long long tile_base) {
+  ImageDesc d{};
+  d.in = c.in;
+  d.out = c.out;
+  d.in_pitch = c.in_pitch;
+  d.out_pitch = c.out_pitch;
+  d.width = c.width;
+  d.height = c.height;
+  d.tile_base = tile_base;
+  d.ntx = (int32_t)((c.width + v->TW - 1) / v->TW);
+  d.nty = (int32_t)((c.height + v->TH - 1) / v->TH);
+  const int cpt = v->TW / 32;
+  const size_t seg_in = (size_t)cpt * in_sz;
+  uint32_t flags = 0;
+  if (((uintptr_t)c.in % seg_in) == 0 && ((size_t)c.in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
+  if (((uintptr_t)c.out % 16) == 0 && ((size_t)c.out_pitch * (16 / cpt)) % 16 == 0) flags |= kOutVec;
+  d.flags = flags;
+  return d;
+}
+
+// ----------------------------------------------------------------------------
+// tuning table: (in, out, mode, dir, log2 w bucket, log2 h bucket, SMs) -> cfg
+// ----------------------------------------------------------------------------
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+std::map<TuneKey, int> g_tune;
+bool g_tune_loaded = false;
+
+int log2_bucket(long long x) {
+  int b = 0;
+  while ((1LL << b) < x && b < 62) ++b;
+  return b;
+}
+
+void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = getenv("SATGB_TUNE_CACHE");
+  if (!path) return;
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  // one entry per line: {"in":0,"out":4,"mode":0,"dir":0,"wb":13,"hb":13,"sms":152,"cfg":1}
+  char line[512];
+  while (fgets(line, sizeof line, f)) {
+    int a[8];
+    if (sscanf(line, " {\"in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"wb\":%d,\"hb\":%d,\"sms\":%d,\"cfg\":%d}",
+               &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7]) == 8)
+      g_tune[TuneKey(a[0], a[1], a[2], a[3], a[4], a[5], a[6])] = a[7];
+  }
+  fclose(f);
+}
+
+void tune_save_locked() {
+  const char* path = getenv("SATGB_TUNE_CACHE");
+  if (!path) return;
+  FILE* f = fopen(path, "w");
+  if (!f) return;
+  for (auto& kv : g_tune) {
+    const TuneKey& k = kv.first;
+    fprintf(f, "{\"in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"wb\":%d,\"hb\":%d,\"sms\":%d,\"cfg\":%d}\n",
+            std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k), std::get<5>(k),
+            std::get<6>(k), kv.second);
+  }
+  fclose(f);
+}
+
+int sms_of(int dev) {
+  auto it = g_dev.find(dev);
+  if (it != g_dev.end()) return it->second.sms;
+  DevInfo d;
+  if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  g_dev.emplace(dev, d);
+  return d.sms;
+}
+
+// Heuristic default when no tuning entry exists: the largest tile whose
+// tile count still gives every SM a few tiles.
+int default_config(long long width, long long height, int sms, int out_sz) {
+  const int cpt = 16 / out_sz;
+  const long long tw = 32LL * cpt;
+  const long long ntx = (width + tw - 1) / tw;
+  const long long tiles128 = ntx * ((height + 127) / 128);
+  const long long tiles64 = ntx * ((height + 63) / 64);
+  if (tiles128 >= 8LL * std::max(1, sms)) return 1;
+  if (tiles64 >= 2LL * std::max(1, sms)) return 0;
+  return 2;
+}
+
+int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, long long h, int dev) {
+  if (g_forced_config >= 0) return g_forced_config;
+  tune_load_locked();
+  const int sms = sms_of(dev);
+  auto it = g_tune.find(TuneKey(in_t, out_t, mode, dir, log2_bucket(w), log2_bucket(h), sms));
+  if (it != g_tune.end()) return it->second;
+  return default_config(w, h, sms, (int)dtype_size(out_t));
+}
+
+satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const ImageDesc& img0,
+                           long long n_images, long long n_tiles, Workspace& ws, int dev,
+                           cudaStream_t s) {
+  const Layout L = layout_for(n_tiles, v);
+  satgb_status st = ensure_ws(ws, L.total, s);
+  if (st != SATGB_OK) return st;
+  int grid = 0;
+  st = grid_for(dev, v, n_tiles, &grid);
+  if (st != SATGB_OK) return st;
+  SatParams P{};
+  P.images = table_dev;
+  P.img0 = img0;
+  P.n_images = n_images;
+  P.n_tiles = n_tiles;
+  char* b = (char*)ws.base;
+  P.ws = (WsHeader*)b;
+  P.row_words = (unsigned long long*)(b + L.row_off);
+  P.col_words = (unsigned long long*)(b + L.col_off);
+  P.corner_words = (unsigned long long*)(b + L.corner_off);
+  P.wait_limit_ns = g_wait_limit_ns.load();
+  P.stall_tile = g_stall_tile.load();
+  cudaError_t e = v->launch(P, grid, s);
+  if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+  g_launches.fetch_add(1);
+  return SATGB_OK;
+}
+
+satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in, long long in_pitch,
+                        void* d_out, long long out_pitch, long long width, long long height,
+                        cudaStream_t s, int force_cfg) {
+  const size_t in_sz = dtype_size(in_t), out_sz = dtype_size(out_t);
+  if (!in_sz || !out_sz) return fail(SATGB_ERR_INVALID_ARG, "unknown dtype code (%d, %d)", in_t, out_t);
+  if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED) return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
+  if (dir != SATGB_FORWARD && dir != SATGB_REVERSE) return fail(SATGB_ERR_INVALID_ARG, "unknown direction %d", dir);
+  if (!pair_offered(in_t, out_t, mode))
+    return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair %s -> %s%s not offered", dtype_name(in_t), dtype_name(out_t),
+                mode == SATGB_MODE_COMPENSATED ? " (compensated)" : "");
+  ImgCheck c{d_in, d_out, in_pitch, out_pitch, width, height};
+  satgb_status st = validate_image(c, in_sz, out_sz);
+  if (st != SATGB_OK) return st;
+  if (width == 0 || height == 0) return SATGB_OK;
+
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  st = get_device(&dev);
+  if (st != SATGB_OK) return st;
+  int cfg = force_cfg >= 0 ? force_cfg : choose_config_locked(in_t, out_t, mode, dir, width, height, dev);
+  const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
+  if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
+  if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
+  ImageDesc d = make_desc(c, v, in_sz, 0);
+  const long long n_tiles = (long long)d.ntx * d.nty;
+  if ((long long)d.ntx * v->TW < width || n_tiles > (1LL << 40))
+    return fail(SATGB_ERR_OVERFLOW, "image too large (%lld x %lld)", width, height);
+  Workspace& ws = g_ws[std::make_pair(dev, (void*)s)];
+  return launch_locked(v, nullptr, d, 1, n_tiles, ws, dev, s);
+}
+
+}  // namespace
+
+// ============================================================================
+// Batch plans
+// ============================================================================
+struct satgb_batch_plan_s {
+  const Variant* v = nullptr;
+  int dev = 0;
+  long long n_images = 0, n_tiles = 0;
+  ImageDesc img0{};
+  ImageDesc* table = nullptr; // device
+  Workspace ws;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+int satgb_version(void) { return SATGB_VERSION; }
+
+const char* satgb_last_error_string(void) { return g_last_error.c_str(); }
+
+int64_t satgb_launch_count(void) { return g_launches.load(); }
+
+satgb_status satgb_set_wait_limit_us(int64_t us) {
+  if (us <= 0) return fail(SATGB_ERR_INVALID_ARG, "wait limit must be positive");
+  g_wait_limit_ns.store(us * 1000LL);
+  return SATGB_OK;
+}
+
+satgb_status satgb_debug_stall_tile(int64_t tile) {
+  g_stall_tile.store(tile < 0 ? -1 : tile);
+  return SATGB_OK;
+}
+
+satgb_status satgb_set_allocator(satgb_alloc_fn alloc_fn, satgb_free_fn free_fn, void* ctx) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if ((alloc_fn == nullptr) != (free_fn == nullptr)) return fail(SATGB_ERR_INVALID_ARG, "allocator needs both functions");
+  g_alloc = alloc_fn;
+  g_free = free_fn;
+  g_alloc_ctx = ctx;
+  return SATGB_OK;
+}
+
+int satgb_num_configs(void) { return kNumConfigs; }
+
+const char* satgb_config_name(int config) {
+  return (config >= 0 && config < kNumConfigs) ? kConfigs[config].name : "";
+}
+
+satgb_status satgb_set_config(int config) {
+  if (config < -1 || config >= kNumConfigs) return fail(SATGB_ERR_INVALID_ARG, "no configuration %d", config);
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_forced_config = config;
+  return SATGB_OK;
+}
+
+satgb_status satgb_scanrow_brlt(satgb_dtype in_t, satgb_dtype out_t, int scan_type, const void* d_in,
+                                int64_t in_pitch, void* d_out, int64_t out_pitch, int64_t width,
+                                int64_t height, satgb_stream stream) {
+  if (scan_type != SATGB_SCAN_KOGGE_STONE && scan_type != SATGB_SCAN_LF)
+    return fail(SATGB_ERR_INVALID_ARG, "scan_type %d is neither KoggeStone_SCAN (0) nor LF_SCAN (1)", scan_type);
+  return sat_single(in_t, out_t, SATGB_MODE_PLAIN, SATGB_FORWARD, d_in, in_pitch, d_out, out_pitch, width,
+                    height, (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_brlt_scanrow(satgb_dtype in_t, satgb_dtype out_t, int scan_type, const void* d_in,
+                                int64_t in_pitch, void* d_out, int64_t out_pitch, int64_t width,
+                                int64_t height, satgb_stream stream) {
+  if (scan_type != SATGB_SCAN_KOGGE_STONE && scan_type != SATGB_SCAN_LF)
+    return fail(SATGB_ERR_INVALID_ARG, "scan_type %d is neither KoggeStone_SCAN (0) nor LF_SCAN (1)", scan_type);
+  return sat_single(in_t, out_t, SATGB_MODE_PLAIN, SATGB_FORWARD, d_in, in_pitch, d_out, out_pitch, width,
+                    height, (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_scanrowcolumn(satgb_dtype in_t, satgb_dtype out_t, int scan_type, const void* d_in,
+                                 int64_t in_pitch, void* d_out, int64_t out_pitch, int64_t width,
+                                 int64_t height, satgb_stream stream) {
+  if (scan_type != SATGB_SCAN_KOGGE_STONE && scan_type != SATGB_SCAN_LF)
+    return fail(SATGB_ERR_INVALID_ARG, "scan_type %d is neither KoggeStone_SCAN (0) nor LF_SCAN (1)", scan_type);
+  return sat_single(in_t, out_t, SATGB_MODE_PLAIN, SATGB_FORWARD, d_in, in_pitch, d_out, out_pitch, width,
+                    height, (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_sat_ex(const satgb_sat_desc* d, satgb_stream stream) {
+  if (!d) return fail(SATGB_ERR_INVALID_ARG, "null descriptor");
+  return sat_single(d->in_t, d->out_t, d->mode, d->direction, d->d_in, d->in_pitch, d->d_out, d->out_pitch,
+                    d->width, d->height, (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream) {
+  if (width <= 0 || height <= 0) return fail(SATGB_ERR_INVALID_ARG, "reserve needs positive sizes");
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  satgb_status st = get_device(&dev);
+  if (st != SATGB_OK) return st;
+  // the largest layout over every variant
+  size_t need = 0;
+  using ListFn = const Variant* (*)(int*);
+  static const ListFn lists[] = {variants_u8, variants_i8, variants_int32, variants_f32, variants_f64};
+  for (ListFn f : lists) {
+    int n = 0;
+    const Variant* v = f(&n);
+    for (int i = 0; i < n; ++i) {
+      long long nt = ((width + v[i].TW - 1) / v[i].TW) * ((height + v[i].TH - 1) / v[i].TH);
+      need = std::max(need, layout_for(nt, &v[i]).total);
+    }
+  }
+  Workspace& ws = g_ws[std::make_pair(dev, (void*)stream)];
+  return ensure_ws(ws, need, (cudaStream_t)stream);
+}
+
+satgb_status satgb_stream_check(satgb_stream stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  satgb_status st = get_device(&dev);
+  if (st != SATGB_OK) return st;
+  satgb_status result = SATGB_OK;
+  auto check = [&](Workspace& ws) {
+    if (!ws.base) return;
+    WsHeader h;
+    if (cudaMemcpy(&h, ws.base, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    if (h.error != 0) {
+      result = fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.error_tile);
+      const uint32_t zero[2] = {0u, 0u};
+      cudaMemcpy((char*)ws.base + offsetof(WsHeader, error), zero, sizeof zero, cudaMemcpyHostToDevice);
+    }
+  };
+  for (auto& kv : g_ws)
+    if (kv.first.first == dev) check(kv.second);
+  return result;
+}
+
+satgb_status satgb_release(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  cudaDeviceSynchronize();
+  for (auto& kv : g_ws) ws_free(kv.second.base);
+  g_ws.clear();
+  return SATGB_OK;
+}
+
+satgb_status satgb_autotune(satgb_dtype in_t, satgb_dtype out_t, int mode, const void* d_in,
+                            int64_t in_pitch, void* d_out, int64_t out_pitch, int64_t width,
+                            int64_t height, satgb_stream stream, int* best_config) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!pair_offered(in_t, out_t, mode)) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair not offered");
+  if (width <= 0 || height <= 0) return fail(SATGB_ERR_INVALID_ARG, "autotune needs a non-empty image");
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  int best = -1;
+  float best_ms = 1e30f;
+  for (int cfg = 0; cfg < kNumConfigs; ++cfg) {
+    if (!find_variant(in_t, out_t, mode, 0, cfg)) continue;
+    satgb_status st = SATGB_OK;
+    for (int i = 0; i < 3 && st == SATGB_OK; ++i)
+      st = sat_single(in_t, out_t, mode, 0, d_in, in_pitch, d_out, out_pitch, width, height, s, cfg);
+    if (st != SATGB_OK) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return st;
+    }
+    const int reps = 10;
+    cudaEventRecord(e0, s);
+    for (int i = 0; i < reps; ++i)
+      sat_single(in_t, out_t, mode, 0, d_in, in_pitch, d_out, out_pitch, width, height, s, cfg);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = cfg;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  satgb_status st = satgb_stream_check(stream);
+  if (st != SATGB_OK) return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  st = get_device(&dev);
+  if (st != SATGB_OK) return st;
+  tune_load_locked();
+  const int sms = sms_of(dev);
+  for (int dir = 0; dir < 2; ++dir)
+    g_tune[TuneKey(in_t, out_t, mode, dir, log2_bucket(width), log2_bucket(height), sms)] = best;
+  tune_save_locked();
+  if (best_config) *best_config = best;
+  return SATGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch plans
+// ---------------------------------------------------------------------------
+satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, satgb_dtype out_t, int mode,
+                                     int direction, const satgb_image* images, int64_t n_images,
+                                     satgb_stream stream) {
+  if (!plan) return fail(SATGB_ERR_INVALID_ARG, "null plan pointer");
+  *plan = nullptr;
+  const size_t in_sz = dtype_size(in_t), out_sz = dtype_size(out_t);
+  if (!in_sz || !out_sz) return fail(SATGB_ERR_INVALID_ARG, "unknown dtype code");
+  if (direction != SATGB_FORWARD && direction != SATGB_REVERSE) return fail(SATGB_ERR_INVALID_ARG, "unknown direction");
+  if (!pair_offered(in_t, out_t, mode)) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair not offered");
+  if (n_images <= 0 || !images) return fail(SATGB_ERR_INVALID_ARG, "empty image list");
+  cudaStream_t s = (cudaStream_t)stream;
+  // Validate every image; empty images are dropped from the table.
+  std::vector<ImgCheck> keep;
+  long long max_w = 0, max_h = 0;
+  double sum_px = 0;
+  for (int64_t i = 0; i < n_images; ++i) {
+    ImgCheck c{images[i].d_in, images[i].d_out, images[i].in_pitch, images[i].out_pitch, images[i].width, images[i].height};
+    satgb_status st = validate_image(c, in_sz, out_sz);
+    if (st != SATGB_OK) return fail(st, "image %lld: %s", (long long)i, g_last_error.c_str());
+    if (c.width > 0 && c.height > 0) {
+      keep.push_back(c);
+      max_w = std::max(max_w, c.width);
+      max_h = std::max(max_h, c.height);
+      sum_px += (double)c.width * (double)c.height;
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  satgb_status st = get_device(&dev);
+  if (st != SATGB_OK) return st;
+  auto* p = new satgb_batch_plan_s();
+  p->dev = dev;
+  // configuration: the tuning entry of the mean image size, else the heuristic
+  const long long side = (long long)std::sqrt(std::max(1.0, sum_px / std::max<size_t>(1, keep.size())));
+  int cfg = g_forced_config >= 0 ? g_forced_config : -1;
+  if (cfg < 0) {
+    tune_load_locked();
+    auto it = g_tune.find(TuneKey(in_t, out_t, mode, direction, log2_bucket(side), log2_bucket(side), sms_of(dev)));
+    cfg = it != g_tune.end() ? it->second : 0;
+  }
+  p->v = find_variant(in_t, out_t, mode, direction, cfg);
+  if (!p->v) p->v = find_variant(in_t, out_t, mode, direction, 0);
+  std::vector<ImageDesc> table;
+  long long base = 0;
+  for (auto& c : keep) {
+    ImageDesc d = make_desc(c, p->v, in_sz, base);
+    base += (long long)d.ntx * d.nty;
+    table.push_back(d);
+  }
+  p->n_images = (long long)table.size();
+  p->n_tiles = base;
+  if (!table.empty()) {
+    p->img0 = table[0];
+    if (cudaMalloc(&p->table, table.size() * sizeof(ImageDesc)) != cudaSuccess) {
+      cudaGetLastError();
+      delete p;
+      return fail(SATGB_ERR_ALLOC, "image table allocation failed");
+    }
+    cudaError_t e = cudaMemcpyAsync(p->table, table.data(), table.size() * sizeof(ImageDesc), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      cudaFree(p->table);
+      delete p;
+      return cuda_fail(e, "image table upload");
+    }
+    st = ensure_ws(p->ws, layout_for(p->n_tiles, p->v).total, s);
+    if (st == SATGB_OK) {
+      e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
+    }
+    if (st == SATGB_OK) {
+      // capture the launch into a graph on a private stream
+      cudaStream_t cs;
+      e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+      if (e == cudaSuccess) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+          const long long before = g_launches.load();
+          st = launch_locked(p->v, p->table, p->img0, p->n_images, p->n_tiles, p->ws, dev, cs);
+          g_launches.store(before); // the capture itself launches nothing
+          cudaError_t e2 = cudaStreamEndCapture(cs, &p->graph);
+          if (st == SATGB_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaStreamEndCapture");
+          if (st == SATGB_OK) {
+            e2 = cudaGraphInstantiate(&p->exec, p->graph, 0);
+            if (e2 != cudaSuccess) st = cuda_fail(e2, "cudaGraphInstantiate");
+          }
+        } else {
+          st = cuda_fail(e, "cudaStreamBeginCapture");
+        }
+        cudaStreamDestroy(cs);
+      } else {
+        st = cuda_fail(e, "cudaStreamCreate");
+      }
+    }
+    if (st != SATGB_OK) {
+      if (p->exec) cudaGraphExecDestroy(p->exec);
+      if (p->graph) cudaGraphDestroy(p->graph);
+      ws_free(p->ws.base);
+      cudaFree(p->table);
+      delete p;
+      return st;
+    }
+  }
+  *plan = p;
+  return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_exec(satgb_batch_plan* p, satgb_stream stream) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  if (p->n_tiles == 0) return SATGB_OK;
+  cudaError_t e = cudaGraphLaunch(p->exec, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+  g_launches.fetch_add(1);
+  return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_launch(satgb_batch_plan* p, satgb_stream stream) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  if (p->n_tiles == 0) return SATGB_OK;
+  std::lock_guard<std::mutex> lk(g_mu);
+  return launch_locked(p->v, p->table, p->img0, p->n_images, p->n_tiles, p->ws, p->dev, (cudaStream_t)stream);
+}
+
+satgb_status satgb_batch_plan_info(const satgb_batch_plan* p, int64_t* n_tiles, int* config) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  if (n_tiles) *n_tiles = p->n_tiles;
+  if (config) *config = p->v ? p->v->cfg : -1;
+  return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_check(satgb_batch_plan* p, satgb_stream stream) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  if (!p->ws.base) return SATGB_OK;
+  WsHeader h;
+  e = cudaMemcpy(&h, p->ws.base, sizeof h, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy");
+  if (h.error) {
+    const uint32_t zero[2] = {0u, 0u};
+    cudaMemcpy((char*)p->ws.base + offsetof(WsHeader, error), zero, sizeof zero, cudaMemcpyHostToDevice);
+    return fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.error_tile);
+  }
+  return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_destroy(satgb_batch_plan* p) {
+  if (!p) return SATGB_OK;
+  cudaDeviceSynchronize();
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  ws_free(p->ws.base);
+  if (p->table) cudaFree(p->table);
+  delete p;
+  return SATGB_OK;
+}
+
+}  // extern "C"

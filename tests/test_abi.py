@@ -1,0 +1,107 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every
+function include/satgb.h declares, and rejects bad arguments before it
+touches the device (the reference has no error reporting at all:
+CUDA_CHECK_ERROR is an empty macro, cudaLib.cuh:21-22)."""
+import ctypes
+import subprocess
+
+import pytest
+
+from sat_gb300 import _lib
+
+
+def test_exports_every_header_symbol(satlib):
+    declared = _lib.header_symbols()
+    assert len(declared) >= 23
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib._build.lib_path()],
+                         capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    for s in declared:
+        assert getattr(satlib, s) is not None
+
+
+def test_version_and_configs(satlib):
+    assert satlib.satgb_version() == 100
+    n = satlib.satgb_num_configs()
+    assert n >= 3
+    assert all(satlib.satgb_config_name(i) for i in range(n))
+    assert satlib.satgb_config_name(n) == b""
+
+
+def _call(satlib, fn, in_t, out_t, scan=0, d_in=0x1000, ip=16, d_out=0x100000, op=16, w=16, h=16):
+    return getattr(satlib, fn)(in_t, out_t, scan, d_in, ip, d_out, op, w, h, None)
+
+
+@pytest.mark.parametrize("fn", ["satgb_scanrow_brlt", "satgb_brlt_scanrow", "satgb_scanrowcolumn"])
+def test_validation_errors(satlib, fn):
+    U8, U32, F32, F64, U16 = _lib.U8, _lib.U32, _lib.F32, _lib.F64, _lib.U16
+    assert _call(satlib, fn, U8, U32, w=-1) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, U8, U32, h=-5) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, U8, U32, scan=2) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, U8, U32, d_in=0) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, U8, U32, d_out=0) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, U8, U32, ip=8) == _lib.ERR_INVALID_ARG          # pitch < width
+    assert _call(satlib, fn, U8, U32, op=15) == _lib.ERR_INVALID_ARG
+    assert _call(satlib, fn, 9, U32) == _lib.ERR_INVALID_ARG                 # unknown dtype code
+    assert _call(satlib, fn, U16, U32) == _lib.ERR_UNSUPPORTED_TYPES        # listed, never dispatched
+    assert _call(satlib, fn, F32, U32) == _lib.ERR_UNSUPPORTED_TYPES        # the reference skips f32->u32
+    assert _call(satlib, fn, F64, F32) == _lib.ERR_UNSUPPORTED_TYPES
+    assert _call(satlib, fn, U8, U32, d_out=0x100002) == _lib.ERR_MISALIGNED
+    assert _call(satlib, fn, U8, U32, d_in=0x1000, d_out=0x1008) == _lib.ERR_INVALID_ARG  # overlap
+    assert _call(satlib, fn, U8, U32, ip=1 << 62, h=1 << 20) == _lib.ERR_OVERFLOW
+    # empty images are a valid no-op and never reach the device
+    assert _call(satlib, fn, U8, U32, w=0) == _lib.OK
+    assert _call(satlib, fn, U8, U32, h=0, d_in=0, d_out=0) == _lib.OK
+    msg = satlib.satgb_last_error_string()
+    assert isinstance(msg, bytes)
+
+
+def test_error_string_set_on_failure(satlib):
+    assert _call(satlib, "satgb_scanrow_brlt", _lib.U8, _lib.U32, w=-1) == _lib.ERR_INVALID_ARG
+    assert b"width" in satlib.satgb_last_error_string()
+
+
+def test_sat_ex_validation(satlib):
+    d = _lib.satgb_sat_desc(_lib.U8, _lib.F32, _lib.MODE_COMPENSATED, _lib.FORWARD, 0x1000, 16, 0x100000, 16, 16, 16)
+    # compensated u8 -> f32 is offered; compensated u8 -> u32 is not
+    d.out_t = _lib.U32
+    assert satlib.satgb_sat_ex(ctypes.byref(d), None) == _lib.ERR_UNSUPPORTED_TYPES
+    d.out_t = _lib.F32
+    d.direction = 3
+    assert satlib.satgb_sat_ex(ctypes.byref(d), None) == _lib.ERR_INVALID_ARG
+    d.direction = 0
+    d.mode = 7
+    assert satlib.satgb_sat_ex(ctypes.byref(d), None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_sat_ex(None, None) == _lib.ERR_INVALID_ARG
+
+
+def test_setters_validate(satlib):
+    assert satlib.satgb_set_config(99) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_set_config(-1) == _lib.OK
+    assert satlib.satgb_set_wait_limit_us(0) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_set_wait_limit_us(2_000_000) == _lib.OK
+    assert satlib.satgb_debug_stall_tile(-1) == _lib.OK
+    alloc = _lib._ALLOC_FN(lambda n, ctx: None)
+    assert satlib.satgb_set_allocator(alloc, _lib._FREE_FN(), None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_set_allocator(_lib._ALLOC_FN(), _lib._FREE_FN(), None) == _lib.OK
+
+
+def test_batch_plan_validation(satlib):
+    plan = ctypes.c_void_p()
+    imgs = (_lib.satgb_image * 1)()
+    imgs[0] = _lib.satgb_image(0x1000, 16, 0x100000, 16, -4, 16)
+    assert satlib.satgb_batch_plan_create(ctypes.byref(plan), _lib.U8, _lib.U32, 0, 0, imgs, 1, None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_batch_plan_create(ctypes.byref(plan), _lib.U8, _lib.U32, 0, 0, imgs, 0, None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_batch_plan_create(None, _lib.U8, _lib.U32, 0, 0, imgs, 1, None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_batch_plan_exec(None, None) == _lib.ERR_INVALID_ARG
+    assert satlib.satgb_batch_plan_destroy(None) == _lib.OK
+
+
+def test_python_api_rejects_cpu_tensors(satlib):
+    torch = pytest.importorskip("torch")
+    import sat_gb300
+    x = torch.zeros(4, 4, dtype=torch.uint8)
+    with pytest.raises(sat_gb300.SatError):
+        sat_gb300.scanrow_brlt(x, torch.uint32)

@@ -1,0 +1,325 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle.
+
+Integer outputs must be bit-exact against the reference's CPU integral image
+(golden vectors made by running it, and the C restatement for other inputs),
+including the mod-2^32 wrap.  Float outputs are judged against the FP64
+oracle with the tolerances below, stated relative to SAT(|a|) computed in
+FP64 (the denominator that stays meaningful under cancellation):
+
+  plain f32       max |S - S64| / SAT(|a|)64  <= 1e-5
+  compensated f32 max |S - S64| / SAT(|a|)64  <= 2e-7   (one final rounding)
+  f64             max |S - S64| / SAT(|a|)64  <= 1e-13
+"""
+import hashlib
+
+import numpy as np
+import pytest
+import torch
+
+import sat_gb300
+from sat_gb300 import _lib
+from tests.util import bits, empty_pitched, to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+TOL = {np.dtype(np.float32): 1e-5, np.dtype(np.float64): 1e-13}
+TOL_COMP = 2e-7
+ALGOS = [sat_gb300.scanrow_brlt, sat_gb300.brlt_scanrow, sat_gb300.scanrowcolumn]
+
+
+def _check_float(oracle, a, s, tol, reverse=False):
+    ref = oracle.sat_fp64(a, reverse=reverse)
+    den = oracle.sat_fp64(a, reverse=reverse, absval=True)
+    err = np.abs(s.astype(np.float64) - ref)
+    mask = den > 0
+    worst = float(np.max(err[mask] / den[mask])) if mask.any() else 0.0
+    assert np.all(err[~mask] == 0)
+    assert worst <= tol, worst
+    return worst
+
+
+def _check(oracle, a, out_np, out_dtype, tol=None, reverse=False):
+    out_dtype = np.dtype(out_dtype)
+    if out_dtype.kind in "iu":
+        ref = oracle.sat_reverse(a, out_dtype) if reverse else oracle.sat_serial(a, out_dtype)
+        assert np.array_equal(bits(out_np), bits(ref))
+    else:
+        _check_float(oracle, a, out_np, tol or TOL[out_dtype], reverse)
+
+
+def test_golden_small_all_entry_points(cuda, oracle, golden):
+    z, meta = golden
+    for case in meta["small"]:
+        a = z[case["key"] + "__in"]
+        r = z[case["key"] + "__out"]
+        x = to_dev(a)
+        for fn in ALGOS:
+            for scan in (sat_gb300.KOGGE_STONE_SCAN, sat_gb300.LF_SCAN):
+                out = to_np(fn(x, torch.float32 if r.dtype == np.float32 else
+                               {np.dtype(np.uint32): torch.uint32, np.dtype(np.int32): torch.int32,
+                                np.dtype(np.float64): torch.float64}[r.dtype], scan_type=scan))
+                if r.dtype.kind in "iu":
+                    assert np.array_equal(bits(out), bits(r)), (case["key"], fn.__name__)
+                else:
+                    _check_float(oracle, a, out, TOL[r.dtype])
+                    _check_float(oracle, a, r, TOL[r.dtype])  # the reference itself meets the same bound
+
+
+def test_reference_size_1024_digests(cuda, oracle, golden):
+    """The reference's smallest benchmark size (1024 x 1024, ScanRow-BRLT.cu:272-273)
+    through all three entry points."""
+    _, meta = golden
+    for case in meta["big"]:
+        ti, to = oracle.PAIRS[case["pair"]]
+        a = oracle.gen(case["kind"], case["seed"], (case["h"], case["w"])).astype(ti)
+        assert hashlib.sha256(a.tobytes()).hexdigest() == case["in_sha256"]
+        x = to_dev(a)
+        for fn in ALGOS:
+            out = to_np(fn(x, {np.dtype(np.uint32): torch.uint32, np.dtype(np.float32): torch.float32,
+                               np.dtype(np.float64): torch.float64}[np.dtype(to)]))
+            if np.dtype(to).kind in "iu":
+                assert hashlib.sha256(out.tobytes()).hexdigest() == case["out_sha256"], (case["key"], fn.__name__)
+            else:
+                _check_float(oracle, a, out, TOL[np.dtype(to)])
+
+
+PAIR_KINDS = {np.uint8: "u8", np.int8: "i8", np.int32: "i32", np.uint32: "u32",
+              np.float32: "f32u", np.float64: "f64u"}
+SHAPES = [(1, 1), (1, 700), (700, 1), (2, 3), (63, 127), (64, 128), (65, 129), (127, 255),
+          (129, 257), (300, 1000), (1000, 300), (517, 769)]
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_all_pairs_all_configs(cuda, oracle, cfg):
+    sat_gb300.set_config(cfg)
+    try:
+        for name, (ti, to) in oracle.PAIRS.items():
+            for i, shape in enumerate(SHAPES):
+                a = oracle.gen(PAIR_KINDS[ti], 1000 + i, shape)
+                out = sat_gb300.sat(to_dev(a), {np.uint32: torch.uint32, np.int32: torch.int32,
+                                                np.float32: torch.float32, np.float64: torch.float64}[to])
+                _check(oracle, a, to_np(out), to)
+    finally:
+        sat_gb300.set_config(-1)
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_reverse_all_configs(cuda, oracle, cfg):
+    sat_gb300.set_config(cfg)
+    try:
+        for name in ("u8_u32", "i32_i32", "f32_f32", "f64_f64", "u8_f64"):
+            ti, to = oracle.PAIRS[name]
+            for i, shape in enumerate(SHAPES):
+                a = oracle.gen(PAIR_KINDS[ti], 2000 + i, shape)
+                out = sat_gb300.sat(to_dev(a), {np.uint32: torch.uint32, np.int32: torch.int32,
+                                                np.float32: torch.float32, np.float64: torch.float64}[to],
+                                    reverse=True)
+                _check(oracle, a, to_np(out), to, reverse=True)
+    finally:
+        sat_gb300.set_config(-1)
+
+
+def test_pitched_unaligned_and_inplace(cuda, oracle):
+    # pitch > width with vector-aligned rows
+    a = oracle.gen("u8", 7, (333, 555))
+    src = empty_pitched(333, 555, 640, torch.uint8)
+    src.copy_(to_dev(a))
+    dst = empty_pitched(333, 555, 600, torch.uint32, fill=-1)
+    sat_gb300.scanrowcolumn(src, torch.uint32, out=dst)
+    assert np.array_equal(to_np(dst), oracle.sat_serial(a, np.uint32))
+    # odd pitch: rows not 4-byte aligned -> scalar loads
+    src2 = empty_pitched(333, 555, 557, torch.uint8)
+    src2.copy_(to_dev(a))
+    dst2 = empty_pitched(333, 555, 559, torch.uint32)
+    sat_gb300.scanrow_brlt(src2, torch.uint32, out=dst2)
+    assert np.array_equal(to_np(dst2), oracle.sat_serial(a, np.uint32))
+    # base pointer offset by one element (misaligned for vectors, aligned for elements)
+    big = torch.zeros(1 + 200 * 300, dtype=torch.uint8, device="cuda")
+    view = big[1:].view(200, 300)
+    b = oracle.gen("u8", 8, (200, 300))
+    view.copy_(to_dev(b))
+    out = sat_gb300.brlt_scanrow(view, torch.uint32)
+    assert np.array_equal(to_np(out), oracle.sat_serial(b, np.uint32))
+    # the padding between rows is never written
+    pad = dst.as_strided((333, 45), (600, 1), dst.storage_offset() + 555)
+    assert np.all(to_np(pad) == np.uint32(0xFFFFFFFF))
+    # in place, f32 -> f32 on one buffer
+    f = oracle.gen("f32u", 9, (400, 700))
+    x = to_dev(f)
+    sat_gb300.sat(x, torch.float32, out=x)
+    _check(oracle, f, to_np(x), np.float32)
+
+
+def test_back_to_back_calls_reuse_workspace(cuda, oracle):
+    rng = np.random.default_rng(0)
+    outs = []
+    for i in range(40):
+        h, w = int(rng.integers(1, 900)), int(rng.integers(1, 900))
+        a = oracle.gen("u8", 3000 + i, (h, w))
+        outs.append((a, sat_gb300.scanrow_brlt(to_dev(a), torch.uint32)))
+    sat_gb300.stream_check()
+    for a, o in outs:
+        assert np.array_equal(to_np(o), oracle.sat_serial(a, np.uint32))
+
+
+def test_other_stream(cuda, oracle):
+    s = torch.cuda.Stream()
+    a = oracle.gen("u8", 44, (1500, 1300))
+    x = to_dev(a)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        out = sat_gb300.scanrowcolumn(x, torch.uint32)
+    s.synchronize()
+    sat_gb300.stream_check(s)
+    assert np.array_equal(to_np(out), oracle.sat_serial(a, np.uint32))
+
+
+@pytest.mark.parametrize("kind", ["f32u", "f32log"])
+def test_compensated_f32(cuda, oracle, kind):
+    a = oracle.gen(kind, 55, (2048, 2048))
+    x = to_dev(a)
+    plain = to_np(sat_gb300.sat(x, torch.float32))
+    comp = to_np(sat_gb300.sat(x, torch.float32, mode="compensated"))
+    ref = oracle.sat_fp64(a)
+    den = oracle.sat_fp64(a, absval=True)
+    e_plain = oracle.err_stats(plain, ref, den)
+    e_comp = oracle.err_stats(comp, ref, den)
+    assert e_plain["max_rel_abs"] <= 1e-5, e_plain
+    assert e_comp["max_rel_abs"] <= TOL_COMP, e_comp
+    if kind == "f32u":
+        assert e_comp["max_rel"] <= 1e-6, e_comp
+    # compensated reverse too
+    rc = to_np(sat_gb300.sat(x, torch.float32, mode="compensated", reverse=True))
+    e_rev = oracle.err_stats(rc, oracle.sat_fp64(a, reverse=True), oracle.sat_fp64(a, reverse=True, absval=True))
+    assert e_rev["max_rel_abs"] <= TOL_COMP, e_rev
+
+
+def test_compensated_u8_and_i8_inputs(cuda, oracle):
+    for kind, dt in (("u8", np.uint8), ("i8", np.int8)):
+        a = oracle.gen(kind, 66, (1000, 1500))
+        comp = to_np(sat_gb300.sat(to_dev(a), torch.float32, mode="compensated"))
+        exact = a.astype(np.int64).cumsum(0).cumsum(1)
+        # integer-valued sums: compensated f32 is the exact sum rounded once
+        assert np.array_equal(comp, exact.astype(np.float32))
+
+
+def test_batch_plan_uneven(cuda, oracle):
+    rng = np.random.default_rng(5)
+    ins, outs, arrs = [], [], []
+    for i in range(48):
+        h = int(np.exp(rng.uniform(np.log(1), np.log(700))))
+        w = int(np.exp(rng.uniform(np.log(1), np.log(700))))
+        a = oracle.gen("u8", 4000 + i, (h, w))
+        arrs.append(a)
+        ins.append(to_dev(a))
+        outs.append(torch.empty((h, w), dtype=torch.uint32, device="cuda"))
+    plan = sat_gb300.BatchPlan(ins, outs)
+    assert plan.info()["n_tiles"] > 48
+    for rep in range(3):
+        for o in outs:
+            o.fill_(0)
+        (plan.exec if rep != 1 else plan.launch)()
+        plan.check()
+        for a, o in zip(arrs, outs):
+            assert np.array_equal(to_np(o), oracle.sat_serial(a, np.uint32))
+    plan.close()
+
+
+def test_batch_plan_float_and_reverse(cuda, oracle):
+    rng = np.random.default_rng(6)
+    ins, outs, arrs = [], [], []
+    for i in range(20):
+        h, w = int(rng.integers(1, 600)), int(rng.integers(1, 600))
+        a = oracle.gen("f32u", 5000 + i, (h, w))
+        arrs.append(a)
+        ins.append(to_dev(a))
+        outs.append(torch.empty((h, w), dtype=torch.float32, device="cuda"))
+    for reverse in (False, True):
+        plan = sat_gb300.BatchPlan(ins, outs, mode="compensated", reverse=reverse)
+        plan.exec()
+        plan.check()
+        for a, o in zip(arrs, outs):
+            _check_float(oracle, a, to_np(o), TOL_COMP, reverse=reverse)
+        plan.close()
+
+
+def test_timeout_is_reported_and_context_survives(cuda, oracle):
+    """A tile that never publishes makes its dependents hit the wait limit;
+    the call reports SATGB_ERR_TIMEOUT and the next call is correct."""
+    L = _lib.load()
+    a = oracle.gen("u8", 77, (512, 512))
+    x = to_dev(a)
+    s = torch.cuda.Stream()
+    try:
+        sat_gb300.set_wait_limit_us(20_000)
+        sat_gb300.set_config(0)
+        assert L.satgb_debug_stall_tile(5) == 0
+        with torch.cuda.stream(s):
+            sat_gb300.scanrow_brlt(x, torch.uint32)
+        with pytest.raises(sat_gb300.SatError) as ei:
+            sat_gb300.stream_check(s)
+        assert ei.value.status == _lib.ERR_TIMEOUT
+    finally:
+        L.satgb_debug_stall_tile(-1)
+        sat_gb300.set_wait_limit_us(2_000_000)
+        sat_gb300.set_config(-1)
+    with torch.cuda.stream(s):
+        out = sat_gb300.scanrow_brlt(x, torch.uint32)
+    sat_gb300.stream_check(s)
+    assert np.array_equal(to_np(out), oracle.sat_serial(a, np.uint32))
+
+
+def test_allocator_hook_failure(cuda, oracle):
+    L = _lib.load()
+    calls = []
+    alloc = _lib._ALLOC_FN(lambda n, ctx: calls.append(n) or None)
+    free = _lib._FREE_FN(lambda p, ctx: None)
+    s = torch.cuda.Stream()  # fresh stream -> fresh workspace
+    assert L.satgb_set_allocator(alloc, free, None) == 0
+    try:
+        x = to_dev(oracle.gen("u8", 1, (64, 64)))
+        with torch.cuda.stream(s):
+            with pytest.raises(sat_gb300.SatError) as ei:
+                sat_gb300.scanrow_brlt(x, torch.uint32)
+        assert ei.value.status == _lib.ERR_ALLOC
+        assert calls
+    finally:
+        assert L.satgb_set_allocator(_lib._ALLOC_FN(), _lib._FREE_FN(), None) == 0
+
+
+def test_launch_count_one_per_call(cuda, oracle):
+    x = to_dev(oracle.gen("u8", 2, (1024, 1024)))
+    before = sat_gb300.launch_count()
+    for fn in ALGOS:
+        fn(x, torch.uint32)
+    assert sat_gb300.launch_count() - before == 3
+
+
+@pytest.mark.slow
+def test_full_size_8192_u8_u32_bit_exact(cuda, oracle):
+    a = oracle.gen("u8", 8192, (8192, 8192))
+    for fn in ALGOS:
+        out = to_np(fn(to_dev(a), torch.uint32))
+        assert np.array_equal(out, oracle.sat_serial(a, np.uint32)), fn.__name__
+
+
+@pytest.mark.slow
+def test_full_size_8192_f32_precision(cuda, oracle):
+    for kind in ("f32u", "f32log"):
+        a = oracle.gen(kind, 8193, (8192, 8192))
+        x = to_dev(a)
+        ref = oracle.sat_fp64(a)
+        den = oracle.sat_fp64(a, absval=True)
+        e_plain = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32)), ref, den)
+        e_comp = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32, mode="compensated")), ref, den)
+        assert e_plain["max_rel_abs"] <= 1e-5, (kind, e_plain)
+        assert e_comp["max_rel_abs"] <= TOL_COMP, (kind, e_comp)
+        if kind == "f32u":
+            assert e_comp["max_rel"] <= 1e-6, e_comp
+
+
+@pytest.mark.slow
+def test_full_size_4096_f64(cuda, oracle):
+    a = oracle.gen("f64u", 4096, (4096, 4096))
+    out = to_np(sat_gb300.sat(to_dev(a), torch.float64))
+    _check_float(oracle, a, out, TOL[np.dtype(np.float64)])
