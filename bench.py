@@ -333,17 +333,60 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+CASES = {
+    # name: (in dtype, out dtype, mode, reverse, height, width)
+    "f32_8192": ("float32", "float32", "plain", False, 8192, 8192),
+    "f32c_8192": ("float32", "float32", "compensated", False, 8192, 8192),
+    "u8_8192": ("uint8", "uint32", "plain", False, 8192, 8192),
+    "f64_4096": ("float64", "float64", "plain", False, 4096, 4096),
+    "f32r_8192": ("float32", "float32", "plain", True, 8192, 8192),
+}
+
+
+def run_case(args):
+    """A few launches of one workload (for ncu captures and quick timing):
+    `--steps` timed launches after `--warmup` untimed ones, median printed."""
+    import torch
+
+    import sat_gb300
+    ti, to, mode, rev, h, w = CASES[args.case]
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    tin, tout = getattr(torch, ti), getattr(torch, to)
+    if tin.is_floating_point:
+        x = torch.rand((h, w), dtype=tin, device=dev, generator=g)
+    else:
+        x = torch.randint(0, 256, (h, w), dtype=tin, device=dev, generator=g)
+    y = torch.empty((h, w), dtype=torch.int32 if tout == torch.uint32 else tout, device=dev)
+    if tout == torch.uint32:
+        y = y.view(torch.uint32)
+    stream = torch.cuda.current_stream()
+    fn = lambda: sat_gb300.sat(x, tout, mode=mode, reverse=rev, out=y)
+    total, per = _time_steps(fn, args.steps, args.warmup, stream, 0.0)
+    sat_gb300.stream_check()
+    nbytes = x.numel() * (x.element_size() + y.element_size())
+    med = statistics.median(per)
+    print(json.dumps({"case": args.case, "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1),
+                      "launches": args.steps + args.warmup}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default=None, choices=sorted(CASES))
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and not args.case:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.case:
+        from sat_gb300 import build as B
+        B.build()
+        run_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         from sat_gb300 import build as B
