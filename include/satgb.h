@@ -139,6 +139,22 @@ typedef struct {
 
 satgb_status satgb_sat_ex(const satgb_sat_desc* desc, satgb_stream stream);
 
+/* The same single-image SAT as satgb_sat_ex, for callers that cannot allocate
+ * device memory: code running inside an allocator or memory-pool callback, in
+ * a process whose device memory a framework has reserved up front, or in a
+ * loop that must not pay for an allocation.  It has no counterpart in the
+ * reference.  It calls no cudaMalloc/cudaFree: its look-back scratch is a
+ * fixed 16 MiB array inside libsatgb.so that every GPU loading the library
+ * holds until the process exits.  Images whose scratch does not fit are
+ * rejected with SATGB_ERR_INVALID_ARG: with the 128-row tiles this entry
+ * point uses, the array holds 8,160 tiles of 128 x 128 pixels for plain
+ * 4-byte outputs (e.g. 8192 x 16256), 4,080 for compensated f32 and 5,433
+ * tiles of 128 x 64 pixels for f64 outputs.  The first call on each device looks up the array's
+ * device address and should come before any stream capture.  All calls share
+ * the array: calls whose kernels overlap on the GPU race and give wrong
+ * results.  Device-side wait timeouts are not reported by this entry point. */
+satgb_status satgb_sat_noalloc(const satgb_sat_desc* desc, satgb_stream stream);
+
 /* ------------------------------------------------------------------------- */
 /* Batched SAT: many images of uneven sizes, one persistent launch.           */
 /* No reference counterpart (the reference's drivers handle one image).       */

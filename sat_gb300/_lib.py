@@ -70,6 +70,7 @@ SIGNATURES = {
     "satgb_brlt_scanrow": (_ST, [_I, _I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "satgb_scanrowcolumn": (_ST, [_I, _I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "satgb_sat_ex": (_ST, [ctypes.POINTER(satgb_sat_desc), _P]),
+    "satgb_sat_noalloc": (_ST, [ctypes.POINTER(satgb_sat_desc), _P]),
     "satgb_batch_plan_create": (_ST, [ctypes.POINTER(_P), _I, _I, _I, _I, ctypes.POINTER(satgb_image), _I64, _P]),
     "satgb_batch_plan_exec": (_ST, [_P, _P]),
     "satgb_batch_plan_launch": (_ST, [_P, _P]),
