@@ -350,6 +350,8 @@ def run_case(args):
 
     import sat_gb300
     ti, to, mode, rev, h, w = CASES[args.case]
+    if args.config >= 0:
+        sat_gb300.set_config(args.config)
     dev = torch.device("cuda", 0)
     g = torch.Generator(device=dev)
     g.manual_seed(7)
@@ -367,13 +369,14 @@ def run_case(args):
     sat_gb300.stream_check()
     nbytes = x.numel() * (x.element_size() + y.element_size())
     med = statistics.median(per)
-    print(json.dumps({"case": args.case, "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1),
+    print(json.dumps({"case": args.case, "config": args.config, "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1),
                       "launches": args.steps + args.warmup}))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default=None, choices=sorted(CASES))
+    ap.add_argument("--config", type=int, default=-1, help="force a tile configuration (--case only)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)

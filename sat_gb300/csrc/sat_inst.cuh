@@ -1,22 +1,46 @@
 // sat_inst.cuh -- helpers for the instantiation translation units.
 #pragma once
+#include <atomic>
+
 #include "sat_kernel.cuh"
 #include "sat_registry.h"
 
 namespace satgb {
 
-template <class TIn, class TOut, class A, bool REV, int RPW>
+// Raises the kernel's dynamic shared-memory limit on the current device (once
+// per device); must precede occupancy queries and launches.
+template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
+cudaError_t prepare_impl() {
+  using SH = TileShape<TIn, TOut, A, RPW, 8>;
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> done[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
+  return e;
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
 cudaError_t launch_impl(const SatParams& p, int grid, cudaStream_t s) {
-  sat_tile_kernel<TIn, TOut, A, REV, RPW, 8><<<grid, 256, 0, s>>>(p);
+  using SH = TileShape<TIn, TOut, A, RPW, 8>;
+  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, MINB>();
+  if (e != cudaSuccess) return e;
+  sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
   return cudaGetLastError();
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW>
-constexpr Variant make_variant(int in_t, int out_t, int mode, int cfg) {
+template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
+Variant make_variant(int in_t, int out_t, int mode, int cfg) {
+  using SH = TileShape<TIn, TOut, A, RPW, 8>;
   return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
-                 &launch_impl<TIn, TOut, A, REV, RPW>,
-                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, 8>,
-                 8 * RPW, 32 * (16 / (int)sizeof(TOut)), Ar<A>::K, 256};
+                 &launch_impl<TIn, TOut, A, REV, RPW, MINB>,
+                 &prepare_impl<TIn, TOut, A, REV, RPW, MINB>,
+                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB>,
+                 SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
 }  // namespace satgb
@@ -30,13 +54,13 @@ constexpr Variant make_variant(int in_t, int out_t, int mode, int cfg) {
 #define SG_F64 7
 
 // all three tile configurations, both directions
-#define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                  \
-  satgb::make_variant<TIN, TOUT, A, false, 8>(IT, OT, MODE, 0),             \
-      satgb::make_variant<TIN, TOUT, A, false, 16>(IT, OT, MODE, 1),        \
-      satgb::make_variant<TIN, TOUT, A, false, 4>(IT, OT, MODE, 2),         \
-      satgb::make_variant<TIN, TOUT, A, true, 8>(IT, OT, MODE, 0),          \
-      satgb::make_variant<TIN, TOUT, A, true, 16>(IT, OT, MODE, 1),         \
-      satgb::make_variant<TIN, TOUT, A, true, 4>(IT, OT, MODE, 2)
+#define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                    \
+  satgb::make_variant<TIN, TOUT, A, false, 8, 2>(IT, OT, MODE, 0),            \
+      satgb::make_variant<TIN, TOUT, A, false, 16, 1>(IT, OT, MODE, 1),       \
+      satgb::make_variant<TIN, TOUT, A, false, 4, 2>(IT, OT, MODE, 2),        \
+      satgb::make_variant<TIN, TOUT, A, true, 8, 2>(IT, OT, MODE, 0),         \
+      satgb::make_variant<TIN, TOUT, A, true, 16, 1>(IT, OT, MODE, 1),        \
+      satgb::make_variant<TIN, TOUT, A, true, 4, 2>(IT, OT, MODE, 2)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

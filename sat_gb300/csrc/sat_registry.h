@@ -1,13 +1,19 @@
-// sat_registry.h -- table of compiled kernel variants (host side).
+// sat_registry.h -- table of compiled kernel variants and host helpers shared
+// by the entry-point translation units.
 #pragma once
-#include <cstdint>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstdint>
 
 namespace satgb {
 
 struct SatParams;
+struct ImageDesc;
 
 using LaunchFn = cudaError_t (*)(const SatParams& p, int grid, cudaStream_t s);
+using PrepareFn = cudaError_t (*)();
 
 // One compiled instantiation of sat_tile_kernel.
 struct Variant {
@@ -16,11 +22,12 @@ struct Variant {
   int dir;         // satgb_direction
   int cfg;         // tile configuration index (see kConfigs)
   LaunchFn launch;
+  PrepareFn prepare;  // sets the dynamic shared-memory limit on the current device
   const void* kernel; // for occupancy queries
-  int TH, TW, K, threads;
+  int TH, TW, K, threads, dyn_smem;
 };
 
-// Tile configurations: rows per warp; every configuration has 8 warps.
+// Tile configurations (rows per consumer warp; 8 consumer warps each).
 struct TileConfig {
   int rows_per_warp;
   const char* name;
@@ -36,5 +43,10 @@ const Variant* variants_f32(int* n);
 const Variant* variants_f64(int* n);
 
 const Variant* find_variant(int in_t, int out_t, int mode, int dir, int cfg);
+
+// Fills `d` for one image (pointers, sizes, tile grid, alignment flags) and,
+// when the input rows are 16-byte aligned, its TMA tensor map.
+void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const void* in, void* out,
+                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base);
 
 }  // namespace satgb

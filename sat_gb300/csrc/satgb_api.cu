@@ -26,10 +26,77 @@
 namespace satgb {
 
 const TileConfig kConfigs[kNumConfigs] = {
-    {8, "tile64x(32*cpt) rpw8"},
-    {16, "tile128x(32*cpt) rpw16"},
-    {4, "tile32x(32*cpt) rpw4"},
+    {8, "64-row tiles (8 rows per warp)"},
+    {16, "128-row tiles (16 rows per warp)"},
+    {4, "32-row tiles (4 rows per warp)"},
 };
+
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+    }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+size_t elem_bytes(int t) {
+  switch (t) {
+    case 0: case 1: return 1;
+    case 2: case 3: return 2;
+    case 4: case 5: case 6: return 4;
+    case 7: return 8;
+    default: return 0;
+  }
+}
+}  // namespace
+
+void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const void* in, void* out,
+                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base) {
+  std::memset(&d, 0, sizeof d);
+  const size_t in_sz = elem_bytes(in_t), out_sz = elem_bytes(out_t);
+  d.in = in;
+  d.out = out;
+  d.in_pitch = in_pitch;
+  d.out_pitch = out_pitch;
+  d.width = width;
+  d.height = height;
+  d.tile_base = tile_base;
+  d.ntx = (int32_t)((width + v->TW - 1) / v->TW);
+  d.nty = (int32_t)((height + v->TH - 1) / v->TH);
+  const int cpt = v->TW / 32;
+  const size_t seg_in = (size_t)cpt * in_sz;
+  uint32_t flags = 0;
+  if (((uintptr_t)in % seg_in) == 0 && ((size_t)in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
+  if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0) flags |= kOutVec;
+  // TMA: 16-byte aligned base and row pitch, extents within 2^32
+  if (((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * in_sz) % 16 == 0 && width < (1LL << 32) &&
+      height < (1LL << 32)) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (enc) {
+      CUtensorMapDataType dt = in_sz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                               : in_t == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                               : in_t == 5 ? CU_TENSOR_MAP_DATA_TYPE_INT32
+                               : in_t == 6 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                           : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+      cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+      cuuint64_t strides[1] = {(cuuint64_t)(in_pitch * (int64_t)in_sz)};
+      cuuint32_t box[2] = {(cuuint32_t)v->TW, (cuuint32_t)v->TH};
+      cuuint32_t estr[2] = {1, 1};
+      CUresult r = enc(&d.tmap_in, dt, 2, const_cast<void*>(in), dims, strides, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r == CUDA_SUCCESS) flags |= kInTma;
+    }
+  }
+  d.flags = flags;
+}
 
 const Variant* find_variant(int in_t, int out_t, int mode, int dir, int cfg) {
   using ListFn = const Variant* (*)(int*);
@@ -183,7 +250,9 @@ satgb_status grid_for(int dev, const Variant* v, long long n_tiles, int* grid) {
   auto jt = g_occ.find(key);
   if (jt == g_occ.end()) {
     int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v->kernel, v->threads, 0);
+    cudaError_t e = v->prepare();
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute");
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v->kernel, v->threads, v->dyn_smem);
     if (e != cudaSuccess) return cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (occ < 1) occ = 1;
     jt = g_occ.emplace(key, occ).first;
@@ -226,26 +295,6 @@ satgb_status validate_image(const ImgCheck& c, size_t in_sz, size_t out_sz) {
   const bool same = ib == ob && in_sz == out_sz && c.in_pitch == c.out_pitch;
   if (!same && ib < oe && ob < ie) return fail(SATGB_ERR_INVALID_ARG, "input and output overlap without being the same buffer");
   return SATGB_OK;
-}
-
-ImageDesc make_desc(const ImgCheck& c, const Variant* v, size_t in_sz, long long tile_base) {
-  ImageDesc d{};
-  d.in = c.in;
-  d.out = c.out;
-  d.in_pitch = c.in_pitch;
-  d.out_pitch = c.out_pitch;
-  d.width = c.width;
-  d.height = c.height;
-  d.tile_base = tile_base;
-  d.ntx = (int32_t)((c.width + v->TW - 1) / v->TW);
-  d.nty = (int32_t)((c.height + v->TH - 1) / v->TH);
-  const int cpt = v->TW / 32;
-  const size_t seg_in = (size_t)cpt * in_sz;
-  uint32_t flags = 0;
-  if (((uintptr_t)c.in % seg_in) == 0 && ((size_t)c.in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
-  if (((uintptr_t)c.out % 16) == 0 && ((size_t)c.out_pitch * (16 / cpt)) % 16 == 0) flags |= kOutVec;
-  d.flags = flags;
-  return d;
 }
 
 // ----------------------------------------------------------------------------
@@ -336,7 +385,8 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
   int grid = 0;
   st = grid_for(dev, v, n_tiles, &grid);
   if (st != SATGB_OK) return st;
-  SatParams P{};
+  SatParams P;
+  std::memset(&P, 0, sizeof P);
   P.images = table_dev;
   P.img0 = img0;
   P.n_images = n_images;
@@ -377,7 +427,8 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
-  ImageDesc d = make_desc(c, v, in_sz, 0);
+  ImageDesc d;
+  fill_image_desc(d, v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, 0);
   const long long n_tiles = (long long)d.ntx * d.nty;
   if ((long long)d.ntx * v->TW < width || n_tiles > (1LL << 40))
     return fail(SATGB_ERR_OVERFLOW, "image too large (%lld x %lld)", width, height);
@@ -394,7 +445,7 @@ struct satgb_batch_plan_s {
   const Variant* v = nullptr;
   int dev = 0;
   long long n_images = 0, n_tiles = 0;
-  ImageDesc img0{};
+  ImageDesc img0;
   ImageDesc* table = nullptr; // device
   Workspace ws;
   cudaGraph_t graph = nullptr;
@@ -630,7 +681,8 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   std::vector<ImageDesc> table;
   long long base = 0;
   for (auto& c : keep) {
-    ImageDesc d = make_desc(c, p->v, in_sz, base);
+    ImageDesc d;
+    fill_image_desc(d, p->v, in_t, out_t, c.in, c.out, c.in_pitch, c.out_pitch, c.width, c.height, base);
     base += (long long)d.ntx * d.nty;
     table.push_back(d);
   }

@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cstddef>
 #include <cstdio>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -145,7 +146,9 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
     sms = g_noalloc_grid_sms[dev];
   }
   int occ = 1;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v->kernel, v->threads, 0);
+  e = v->prepare();
+  if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, v->kernel, v->threads, v->dyn_smem);
   if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
   if (occ < 1) occ = 1;
   const int grid = (int)std::max(1LL, std::min((long long)sms * occ, n_tiles));
@@ -156,24 +159,11 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
   if (e == cudaSuccess) e = cudaMemsetAsync((char*)base + offsetof(WsHeader, error), 0, 2 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
 
-  ImageDesc img{};
-  img.in = d->d_in;
-  img.out = d->d_out;
-  img.in_pitch = d->in_pitch;
-  img.out_pitch = d->out_pitch;
-  img.width = d->width;
-  img.height = d->height;
-  img.tile_base = 0;
-  img.ntx = (int32_t)ntx;
-  img.nty = (int32_t)nty;
-  const int cpt = v->TW / 32;
-  const size_t seg_in = (size_t)cpt * in_sz;
-  uint32_t flags = 0;
-  if (((uintptr_t)d->d_in % seg_in) == 0 && ((size_t)d->in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
-  if (((uintptr_t)d->d_out % 16) == 0 && ((size_t)d->out_pitch * out_sz) % 16 == 0) flags |= kOutVec;
-  img.flags = flags;
+  ImageDesc img;
+  fill_image_desc(img, v, d->in_t, d->out_t, d->d_in, d->d_out, d->in_pitch, d->out_pitch, d->width, d->height, 0);
 
-  SatParams P{};
+  SatParams P;
+  std::memset(&P, 0, sizeof P);
   P.images = nullptr;
   P.img0 = img;
   P.n_images = 1;
