@@ -9,37 +9,37 @@ namespace satgb {
 
 // Raises the kernel's dynamic shared-memory limit on the current device (once
 // per device); must precede occupancy queries and launches.
-template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
 cudaError_t prepare_impl() {
-  using SH = TileShape<TIn, TOut, A, RPW, 8>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   constexpr int kMaxDev = 64;
   static std::atomic<int> done[kMaxDev];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
-  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB>,
+  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
   if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
   return e;
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
 cudaError_t launch_impl(const SatParams& p, int grid, cudaStream_t s) {
-  using SH = TileShape<TIn, TOut, A, RPW, 8>;
-  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, MINB>();
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
+  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB>();
   if (e != cudaSuccess) return e;
-  sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
   return cudaGetLastError();
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
 Variant make_variant(int in_t, int out_t, int mode, int cfg) {
-  using SH = TileShape<TIn, TOut, A, RPW, 8>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
-                 &launch_impl<TIn, TOut, A, REV, RPW, MINB>,
-                 &prepare_impl<TIn, TOut, A, REV, RPW, MINB>,
-                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, 8, MINB>,
+                 &launch_impl<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 &prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB>,
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
@@ -53,14 +53,18 @@ Variant make_variant(int in_t, int out_t, int mode, int cfg) {
 #define SG_F32 6
 #define SG_F64 7
 
-// all three tile configurations, both directions
+// every tile configuration, both directions:
+//   0: 64-row tiles, 8 warps, 2 CTAs/SM     1: 128-row tiles, 8 warps
+//   2: 32-row tiles, 8 warps                3: 128-row tiles, 16 warps, 1 CTA/SM
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                    \
-  satgb::make_variant<TIN, TOUT, A, false, 8, 2>(IT, OT, MODE, 0),            \
-      satgb::make_variant<TIN, TOUT, A, false, 16, 1>(IT, OT, MODE, 1),       \
-      satgb::make_variant<TIN, TOUT, A, false, 4, 2>(IT, OT, MODE, 2),        \
-      satgb::make_variant<TIN, TOUT, A, true, 8, 2>(IT, OT, MODE, 0),         \
-      satgb::make_variant<TIN, TOUT, A, true, 16, 1>(IT, OT, MODE, 1),        \
-      satgb::make_variant<TIN, TOUT, A, true, 4, 2>(IT, OT, MODE, 2)
+  satgb::make_variant<TIN, TOUT, A, false, 8, 8, 2>(IT, OT, MODE, 0),         \
+      satgb::make_variant<TIN, TOUT, A, false, 16, 8, 1>(IT, OT, MODE, 1),    \
+      satgb::make_variant<TIN, TOUT, A, false, 4, 8, 2>(IT, OT, MODE, 2),     \
+      satgb::make_variant<TIN, TOUT, A, false, 8, 16, 1>(IT, OT, MODE, 3),    \
+      satgb::make_variant<TIN, TOUT, A, true, 8, 8, 2>(IT, OT, MODE, 0),      \
+      satgb::make_variant<TIN, TOUT, A, true, 16, 8, 1>(IT, OT, MODE, 1),     \
+      satgb::make_variant<TIN, TOUT, A, true, 4, 8, 2>(IT, OT, MODE, 2),      \
+      satgb::make_variant<TIN, TOUT, A, true, 8, 16, 1>(IT, OT, MODE, 3)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

@@ -60,7 +60,8 @@
 namespace satgb {
 
 struct ImageDesc {
-  CUtensorMap tmap_in; // 2-D tiled map of the input (valid when flags & kInTma)
+  CUtensorMap tmap_in;  // 2-D tiled map of the input (valid when flags & kInTma)
+  CUtensorMap tmap_out; // 2-D tiled map of the output (valid when flags & kOutTma)
   const void* in;
   void* out;
   int64_t in_pitch;  // elements
@@ -68,12 +69,13 @@ struct ImageDesc {
   int64_t width, height;
   int64_t tile_base; // global index of the image's first tile
   int32_t ntx, nty;  // tiles across / down
-  uint32_t flags;    // kInVec | kOutVec | kInTma
+  uint32_t flags;    // kInVec | kOutVec | kInTma | kOutTma
   uint32_t pad;
 };
 constexpr uint32_t kInVec = 1u;  // every thread's CPT-element input row segment is vector-aligned
 constexpr uint32_t kOutVec = 2u; // every 16-byte output row segment is aligned
 constexpr uint32_t kInTma = 4u;  // tmap_in is valid: tiles arrive by TMA
+constexpr uint32_t kOutTma = 8u; // tmap_out is valid: results leave by TMA
 
 struct SatParams {
   ImageDesc img0;          // the image when n_images == 1
@@ -88,10 +90,15 @@ struct SatParams {
   int64_t stall_tile; // test knob: this tile never publishes (-1: none)
 };
 
-// Pipeline depth: enough stages for ~64 KB of input in flight per CTA.
-template <int STAGE_BYTES>
+// Pipeline depth.  A stage holds one tile from its TMA load until its TMA
+// store has read the results back out of it, so a CTA cycles through S
+// stages: as many as fit in its share of the SM's 227 KB of shared memory
+// (CTAS CTAs per SM) next to its static shared memory, between 2 and 6.
+template <int STAGE_BYTES, int STATIC_BYTES, int CTAS>
 struct Stages {
-  static constexpr int value = STAGE_BYTES >= 32768 ? 2 : (STAGE_BYTES >= 16384 ? 3 : 4);
+  static constexpr int budget = (CTAS == 1 ? 227 * 1024 : 113 * 1024) - STATIC_BYTES - 1024;
+  static constexpr int fit = budget / STAGE_BYTES;
+  static constexpr int value = fit < 2 ? 2 : (fit > 6 ? 6 : fit);
 };
 
 template <int BYTES>
@@ -123,6 +130,17 @@ __device__ __forceinline__ void load_seg(const TIn* p, bool vec, int nvalid, TIn
     for (int c = 0; c < CPT; ++c) x[c] = (c < nvalid) ? __ldcs(p + c) : TIn(0);
   }
 }
+
+// One thread's CPT input elements of one row, kept packed in registers
+// (a single 32-bit register for four 8-bit pixels).
+template <class TIn, int CPT>
+struct RowSeg {
+  using V = typename VecT<CPT * sizeof(TIn)>::T;
+  union {
+    V v;
+    TIn e[CPT];
+  } u;
+};
 
 template <class TIn, int CPT>
 __device__ __forceinline__ void load_seg_smem(const TIn* p, TIn (&x)[CPT]) {
@@ -186,6 +204,17 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
       : "memory");
 }
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// Waits until every bulk store this thread committed has finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Waits until every bulk store this thread committed is complete.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
@@ -265,67 +294,136 @@ __device__ __forceinline__ void diag_tile(long long k, int ntx, int nty, int& tx
   tx = (int)(d - ty);
 }
 
-// Windowed look-back.  At the start of a tile the look-back thread of a vector
-// element (or of the corner) loads the status words of its W nearest
-// predecessors -- one round trip that overlaps the tile's local phase.  After
-// the local phase, resolve() walks those values (aggregates are summed until an
-// inclusive value is found) and only goes back to memory, with waiting reads,
-// for predecessors that were not ready or lie beyond the window.
+// Windowed look-back.  The look-back thread of a vector element (or of the
+// corner) reads the status words of W predecessors at once -- one round trip
+// for W tiles.  It walks the window from the nearest predecessor, summing
+// aggregates until it meets an inclusive value; when it reaches a predecessor
+// that has published nothing yet, it reads the window again, now starting at
+// that predecessor.  So an inclusive value W tiles back is found in one round
+// trip as long as the tiles in between have published their aggregates, which
+// they do right after their local phase.  The first window is read when the
+// tile starts, overlapping the local phase.
 template <class A>
 struct EarlyWin {
-  static constexpr int W = Ar<A>::K == 1 ? 3 : 2;
+  static constexpr int W = Ar<A>::K == 1 ? 4 : 3;
   unsigned long long w[W][Ar<A>::K];
 };
 
 template <class A>
 __device__ __forceinline__ void early_read(EarlyWin<A>& e, const unsigned long long* base, long long stride,
-                                           int steps) {
+                                           int steps, int first = 0) {
   constexpr int K = Ar<A>::K;
 #pragma unroll
-  for (int i = 0; i < EarlyWin<A>::W; ++i) {
+  for (int q = 0; q < EarlyWin<A>::W; ++q) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) e.w[i][k] = (i < steps) ? ld_relaxed_u64(base + (i + 1) * stride + k) : 0ull;
+    for (int k = 0; k < K; ++k)
+      e.w[q][k] = (first + q < steps) ? ld_relaxed_u64(base + (first + q + 1) * stride + k) : 0ull;
   }
+}
+
+// 0 = not published yet, else kStateAgg / kStateInc with the value in `val`.
+template <class A>
+__device__ __forceinline__ uint32_t decode_word(const unsigned long long (&w)[Ar<A>::K], uint32_t tagA, uint32_t tagI,
+                                                A& val) {
+  constexpr int K = Ar<A>::K;
+  const uint32_t tag = (uint32_t)(w[0] >> 32);
+  bool ok = (tag == tagA || tag == tagI);
+  uint32_t pl[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    ok = ok && ((uint32_t)(w[k] >> 32) == tag);
+    pl[k] = (uint32_t)w[k];
+  }
+  if (!ok) return 0u;
+  val = Ar<A>::from_words(pl);
+  return tag & 3u;
 }
 
 template <class A>
-__device__ __forceinline__ A resolve(const EarlyWin<A>& e, const unsigned long long* base, long long stride,
-                                     int steps, uint32_t tagA, uint32_t tagI, const SatParams& P, long long tile) {
-  constexpr int K = Ar<A>::K;
+__device__ __forceinline__ A resolve(EarlyWin<A>& e, const unsigned long long* base, long long stride, int steps,
+                                     uint32_t tagA, uint32_t tagI, const SatParams& P, long long tile) {
+  constexpr int W = EarlyWin<A>::W;
   A acc = Ar<A>::zero();
-  int i = 0;
+  int i = 0; // predecessors already accounted for
+  unsigned long long t0 = 0;
+  unsigned ns = 0;
+  for (uint32_t round = 0;; ++round) {
+    bool progressed = false;
 #pragma unroll
-  for (int q = 0; q < EarlyWin<A>::W; ++q) {
-    if (i != q || q >= steps) break;
-    const uint32_t tag = (uint32_t)(e.w[q][0] >> 32);
-    bool ok = (tag == tagA || tag == tagI);
-    uint32_t pl[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      ok = ok && ((uint32_t)(e.w[q][k] >> 32) == tag);
-      pl[k] = (uint32_t)e.w[q][k];
+    for (int q = 0; q < W; ++q) {
+      if (i >= steps) return acc;
+      A val;
+      const uint32_t st = decode_word<A>(e.w[q], tagA, tagI, val);
+      if (!st) break;
+      acc = Ar<A>::add(val, acc);
+      ++i;
+      progressed = true;
+      if (st == kStateInc) return acc;
     }
-    if (!ok) break;
-    acc = Ar<A>::add(Ar<A>::from_words(pl), acc);
-    if (tag == tagI) return acc;
-    ++i;
+    if (i >= steps) return acc;
+    if (!progressed) {
+      // the nearest open predecessor has published nothing yet: back off, bounded
+      if (t0 == 0) t0 = global_timer_ns();
+      if (ns) __nanosleep(ns);
+      ns = ns ? (ns < 256 ? 2 * ns : ns) : 32;
+      if ((round & 7u) == 7u &&
+          ((long long)(global_timer_ns() - t0) > P.wait_limit_ns || ld_relaxed_u32(&P.ws->error) != 0u)) {
+        record_error(P, tile);
+        return acc;
+      }
+    }
+    early_read<A>(e, base, stride, steps, i);
   }
-  for (; i < steps; ++i) {
-    A val;
-    const uint32_t sr = wait_read<A>(base + (i + 1) * stride, tagA, tagI, val, P, tile);
-    acc = Ar<A>::add(val, acc);
-    if (sr == kStateInc) break;
-  }
-  return acc;
 }
 
-template <class TIn, class TOut, class A, int RPW, int NW>
+// The fields of an image descriptor a tile needs, in registers.  For a single
+// image they are read straight from the kernel parameter (constant bank);
+// only batched launches read the descriptor table in global memory.
+struct ImageView {
+  const void* in;
+  void* out;
+  int64_t in_pitch, out_pitch, width, height;
+  int32_t ntx, nty;
+  uint32_t flags;
+};
+
+__device__ __forceinline__ ImageView image_view(const SatParams& P, int img) {
+  ImageView v;
+  if (P.n_images == 1) {
+    v.in = P.img0.in;
+    v.out = P.img0.out;
+    v.in_pitch = P.img0.in_pitch;
+    v.out_pitch = P.img0.out_pitch;
+    v.width = P.img0.width;
+    v.height = P.img0.height;
+    v.ntx = P.img0.ntx;
+    v.nty = P.img0.nty;
+    v.flags = P.img0.flags;
+  } else {
+    const ImageDesc* D = &P.images[img];
+    v.in = D->in;
+    v.out = D->out;
+    v.in_pitch = D->in_pitch;
+    v.out_pitch = D->out_pitch;
+    v.width = D->width;
+    v.height = D->height;
+    v.ntx = D->ntx;
+    v.nty = D->nty;
+    v.flags = D->flags;
+  }
+  return v;
+}
+
+template <class TIn, class TOut, class A, int RPW, int NW, int CTAS>
 struct TileShape {
   static constexpr int CPT = 16 / (int)sizeof(TOut);
   static constexpr int TW = 32 * CPT;
   static constexpr int TH = NW * RPW;
-  static constexpr int STAGE_BYTES = TH * TW * (int)sizeof(TIn);
-  static constexpr int S = Stages<STAGE_BYTES>::value;
+  static constexpr int IN_BYTES = TH * TW * (int)sizeof(TIn); // what the TMA load brings
+  static constexpr int STAGE_BYTES = TH * TW * (int)(sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
+  // static shared memory of the kernel (s_tr, s_colp, the vectors), roughly
+  static constexpr int STATIC_BYTES = (NW * RPW * 33 + NW * TW + 3 * TH + TW) * (int)sizeof(A) + 256;
+  static constexpr int S = Stages<STAGE_BYTES, STATIC_BYTES, CTAS>::value;
   static constexpr int DYN_SMEM = S * STAGE_BYTES;
   static constexpr int THREADS = NW * 32;
 };
@@ -371,33 +469,59 @@ __device__ __forceinline__ bool produce(const SatParams& P, unsigned long long t
   return true;
 }
 
+// ---------------------------------------------------------------------------
+// The tile kernel.  Per tile, with the tile resident in a shared-memory stage:
+//
+//  A  aggregates: each thread sums its CPT-column x RPW-row block by columns
+//     (colp) and by rows (rowp).  A transpose through shared memory turns the
+//     32 lanes' row partials of each row into the exclusive prefix E over the
+//     lanes (kept in registers) and the row total (the tile's row aggregate).
+//     Column partials go to shared memory.  Then one barrier.
+//  B  look-backs: threads [0,TW) sum the column partials into the tile's
+//     column aggregate (published), turn them into the exclusive prefix over
+//     warps C_w, and look back up the column; threads [TW,TW+TH) publish the
+//     row aggregate and look back along the row; a spare warp looks back over
+//     the corner words; a spare thread takes the next ticket and starts the
+//     next tile's TMA load.  The row group then scans rowleft over the rows
+//     (RL) and computes u = sum rowleft; with the corner known the corner's
+//     inclusive value is published right away.
+//  D  scan + store: warp w forms the SAT row just above its rows,
+//        Top_w(x) = corner + RL(above the warp) + sum_{x0<=i<=x} (colabove(i) + C_w(i)),
+//     then walks its rows once: run = rowleft(y) + E(y) + in-thread row prefix,
+//     acc(x) += run, and stores acc.  About four additions per element.
+//
+// The reverse (suffix) SAT runs every scan in the opposite direction.
+// ---------------------------------------------------------------------------
 template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
 __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_constant__ SatParams P) {
-  using SH = TileShape<TIn, TOut, A, RPW, NW>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   constexpr int CPT = SH::CPT;
   constexpr int TW = SH::TW;
   constexpr int TH = SH::TH;
   constexpr int S = SH::S;
   constexpr int NC = NW * 32;
-  constexpr int STAGE_ELEMS = TH * TW;
-  constexpr int PT = NC - 1; // producer thread: idle in the look-back phase when TW + TH < NC
-  // corner look-back thread: a spare thread when there is one, else thread 0 after its column
-  constexpr int CT = (TW + TH < NC - 1) ? TW + TH : 0;
-  static_assert(TW + TH <= NC, "one thread per row and per column of the tile");
+  constexpr int STAGE_ELEMS = SH::STAGE_BYTES / (int)sizeof(TIn); // stage stride in input elements
+  constexpr int SPARE = NC - (TW + TH);
+  static_assert(SPARE >= 0, "one thread per row and per column of the tile");
   static_assert(TH % 32 == 0 && TW % 32 == 0, "groups are whole warps");
+  static_assert(32 % RPW == 0, "rows per warp divide the warp");
+  constexpr bool CORNER_WARP = SPARE >= 64; // a spare warp for the corner, another one holds the producer
+  constexpr int CW = (TW + TH) / 32;        // that corner warp
+  constexpr int PT = NC - 1;                // producer thread
+  constexpr int LPR = 32 / RPW;             // transpose-scan: lanes per row ...
+  constexpr int CH = RPW;                   // ... and values per lane
   constexpr int K = Ar<A>::K;
   using AR = Ar<A>;
 
   extern __shared__ __align__(128) unsigned char dsmem[];
   TIn* stages = reinterpret_cast<TIn*>(dsmem);
 
-  __shared__ A s_bot[2][NW][TW];    // per warp: column sums of its row-scanned rows, then the cross-warp carry
-  __shared__ A s_colraw[2][NW][TW]; // per warp: column sums of the raw input
-  __shared__ A s_rowagg[2][TH];     // row sums of the tile
+  __shared__ A s_tr[NW][RPW][33];   // per-warp transpose scratch for the row offsets
+  __shared__ A s_colp[NW][TW];      // per warp: raw column partials (by slot); then the exclusive prefix over warps
+  __shared__ A s_rowagg[TH];        // row totals of the tile
   __shared__ A s_rowleft[TH];       // row look-back result
-  __shared__ A s_RL[TH];            // scan over the tile's rows of rowleft
+  __shared__ A s_RL[TH];            // scan of rowleft over the tile's rows
   __shared__ A s_colabove[TW];      // column look-back result (by slot)
-  __shared__ A s_CA[TW];            // scan over the tile's columns of colabove (by slot)
   __shared__ A s_corner, s_u;
   __shared__ long long s_tile[S];   // spatial tile index per stage (-1: no more tiles)
   __shared__ int s_img[S];
@@ -418,9 +542,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     for (int s = 0; s < S; ++s) mbar_init(smem_u32(&s_full[s]), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 #pragma unroll
-    for (int s = 0; s < S; ++s) {
+    for (int s = 0; s < S - 1; ++s) {
       if (producing)
-        producing = produce<TIn, REV, TW, TH, SH::STAGE_BYTES>(P, atomicAdd(&P.ws->ticket, 1ull), s,
+        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, atomicAdd(&P.ws->ticket, 1ull), s,
                                                                stages + s * STAGE_ELEMS, s_tile, s_img, s_tx,
                                                                s_ty, s_full);
     }
@@ -428,255 +552,281 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   }
   __syncthreads();
 
-  {
-    for (int k = 0;; ++k) {
-      const int st = k % S;
-      const int buf = k & 1;
-      mbar_wait_bounded(smem_u32(&s_full[st]), (k / S) & 1, P, -1);
-      const long long t = s_tile[st];
-      if (t < 0) break;
-      const int tx = s_tx[st], ty = s_ty[st];
-      const ImageDesc* Dp = (P.n_images == 1) ? &P.img0 : &P.images[s_img[st]];
-      const int64_t width = Dp->width, height = Dp->height;
-      const int64_t out_pitch = Dp->out_pitch;
-      const int ntx = Dp->ntx, nty = Dp->nty;
-      const uint32_t flags = Dp->flags;
+  for (int k = 0;; ++k) {
+    const int st = k % S;
+    mbar_wait_bounded(smem_u32(&s_full[st]), (k / S) & 1, P, -1);
+    const long long t = s_tile[st];
+    if (t < 0) break;
+    const int tx = s_tx[st], ty = s_ty[st];
+    const int img = s_img[st];
+    const ImageView Dp = image_view(P, img);
+    const int ntx = Dp.ntx, nty = Dp.nty;
+    const uint32_t flags = Dp.flags;
+    const long long x0 = (long long)tx * TW;
+    const long long y0 = (long long)ty * TH;
+    const long long xt = x0 + (long long)lane * CPT;
+    const long long rem = Dp.width - xt;
+    const int nvalid = rem <= 0 ? 0 : (rem >= CPT ? CPT : (int)rem);
+    TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT; // this thread's block in the stage
 
-      const long long x0 = (long long)tx * TW;
-      const long long y0 = (long long)ty * TH;
-      const long long xt = x0 + (long long)lane * CPT;
-      const long long rem = width - xt;
-      const int nvalid = rem <= 0 ? 0 : (rem >= CPT ? CPT : (int)rem);
+    // early look-back reads: the W nearest predecessors of this thread's element
+    const int col_steps = REV ? (nty - 1 - ty) : ty;
+    const int row_steps = REV ? (ntx - 1 - tx) : tx;
+    EarlyWin<A> early;
+    const unsigned long long* lb_base = nullptr;
+    long long lb_stride = 0;
+    int lb_steps = 0;
+    if (tid < TW) {
+      lb_base = P.col_words + ((unsigned long long)t * TW + tid) * K;
+      lb_stride = (REV ? 1 : -1) * (long long)ntx * TW * K;
+      lb_steps = col_steps;
+    } else if (tid < TW + TH) {
+      lb_base = P.row_words + ((unsigned long long)t * TH + (tid - TW)) * K;
+      lb_stride = (REV ? 1 : -1) * (long long)TH * K;
+      lb_steps = row_steps;
+    } else if ((CORNER_WARP && warp == CW && lane == 0) || (!CORNER_WARP && tid == 0)) {
+      lb_base = P.corner_words + (unsigned long long)t * K;
+      lb_stride = (REV ? 1 : -1) * (long long)ntx * K;
+      lb_steps = col_steps;
+    }
+    EarlyWin<A> early_c; // thread 0's corner window when there is no corner warp
+    if (lb_base) early_read<A>(early, lb_base, lb_stride, lb_steps);
+    const unsigned long long* cb_base = P.corner_words + (unsigned long long)t * K;
+    const long long cb_stride = (REV ? 1 : -1) * (long long)ntx * K;
+    if (!CORNER_WARP && tid == 0) early_read<A>(early_c, cb_base, cb_stride, col_steps);
 
-      // early look-back reads: the W nearest predecessors of this thread's element
-      const int col_steps = REV ? (nty - 1 - ty) : ty;
-      const int row_steps = REV ? (ntx - 1 - tx) : tx;
-      EarlyWin<A> early, early_c;
-      const unsigned long long* lb_base = nullptr;
-      long long lb_stride = 0;
-      int lb_steps = 0;
-      if (tid < TW) {
-        lb_base = P.col_words + ((unsigned long long)t * TW + tid) * K;
-        lb_stride = (REV ? 1 : -1) * (long long)ntx * TW * K;
-        lb_steps = col_steps;
-      } else if (tid < TW + TH) {
-        lb_base = P.row_words + ((unsigned long long)t * TH + (tid - TW)) * K;
-        lb_stride = (REV ? 1 : -1) * (long long)TH * K;
-        lb_steps = row_steps;
-      }
-      if (lb_base) early_read<A>(early, lb_base, lb_stride, lb_steps);
-      const unsigned long long* cb_base = P.corner_words + (unsigned long long)t * K;
-      const long long cb_stride = (REV ? 1 : -1) * (long long)ntx * K;
-      if (tid == CT) early_read<A>(early_c, cb_base, cb_stride, col_steps);
-
-      // ---- phase A: load, local row scans, local column scans ---------------
-      A v[RPW][CPT];
-      A colraw[CPT];
+    // ---- phase A: aggregates --------------------------------------------------
+    // the thread's block stays in registers (packed) until phase D, so the
+    // stage is free for the next tile's TMA as soon as phase A ends
+    RowSeg<TIn, CPT> raw[RPW];
+    A colp[CPT], rowp[RPW];
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) colraw[c] = AR::zero();
-      if (flags & kInTma) {
-        const TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
-#pragma unroll
-        for (int r = 0; r < RPW; ++r) {
-          TIn x[CPT];
-          load_seg_smem<TIn, CPT>(sb + r * TW, x);
-#pragma unroll
-          for (int c = 0; c < CPT; ++c) {
-            v[r][c] = Cvt<A, TIn>::in(x[c]);
-            colraw[c] = AR::add(colraw[c], v[r][c]);
-          }
-        }
-      } else {
-        const TIn* in = static_cast<const TIn*>(Dp->in);
-        const int64_t in_pitch = Dp->in_pitch;
-        const bool vin = (flags & kInVec) && nvalid == CPT;
-#pragma unroll
-        for (int r = 0; r < RPW; ++r) {
-          const long long y = y0 + warp * RPW + r;
-          TIn x[CPT];
-          if (y < height && nvalid > 0) {
-            load_seg<TIn, CPT>(in + y * in_pitch + xt, vin, nvalid, x);
-          } else {
-#pragma unroll
-            for (int c = 0; c < CPT; ++c) x[c] = TIn(0);
-          }
-#pragma unroll
-          for (int c = 0; c < CPT; ++c) {
-            v[r][c] = Cvt<A, TIn>::in(x[c]);
-            colraw[c] = AR::add(colraw[c], v[r][c]);
-          }
-        }
-      }
-      // row scans, all RPW rows interleaved step by step (independent chains)
-      A incl[RPW];
+    for (int c = 0; c < CPT; ++c) colp[c] = AR::zero();
+    {
+      const bool tma = flags & kInTma;
+      const TIn* gin = static_cast<const TIn*>(Dp.in) + (y0 + warp * RPW) * Dp.in_pitch + xt;
+      const bool vin = (flags & kInVec) && nvalid == CPT;
 #pragma unroll
       for (int r = 0; r < RPW; ++r) {
+        if (tma) {
+          raw[r].u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+        } else if (y0 + warp * RPW + r < Dp.height && nvalid > 0) {
+          load_seg<TIn, CPT>(gin + r * Dp.in_pitch, vin, nvalid, raw[r].u.e);
+        } else {
 #pragma unroll
-        for (int i = 1; i < CPT; ++i) {
-          const int c = REV ? CPT - 1 - i : i;
-          const int p = REV ? c + 1 : c - 1;
-          v[r][c] = AR::add(v[r][p], v[r][c]);
+          for (int c = 0; c < CPT; ++c) raw[r].u.e[c] = TIn(0);
         }
-        incl[r] = v[r][REV ? 0 : CPT - 1];
+        A rs = AR::zero();
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+          const A a = Cvt<A, TIn>::in(raw[r].u.e[c]);
+          colp[c] = AR::add(colp[c], a);
+          rs = AR::add(rs, a);
+        }
+        rowp[r] = rs;
       }
+    }
+    // row partials -> exclusive prefix over the lanes (E) and the row totals
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) s_tr[warp][r][lane] = rowp[r];
+    __syncwarp();
+    {
+      const int r = lane / LPR, q = lane % LPR;
+      A tot = AR::zero();
+#pragma unroll
+      for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][q * CH + (REV ? CH - 1 - i : i)]);
+      A incl = tot;
+#pragma unroll
+      for (int d = 1; d < LPR; d <<= 1) {
+        const A o = REV ? AR::shfl_down(incl, d, LPR) : AR::shfl_up(incl, d, LPR);
+        if (REV ? (q + d < LPR) : (q >= d)) incl = AR::add(o, incl);
+      }
+      A ex = REV ? AR::shfl_down(incl, 1, LPR) : AR::shfl_up(incl, 1, LPR);
+      if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        const int idx = q * CH + (REV ? CH - 1 - i : i);
+        const A vv = s_tr[warp][r][idx];
+        s_tr[warp][r][idx] = ex;
+        ex = AR::add(ex, vv);
+      }
+      if (q == (REV ? 0 : LPR - 1)) s_rowagg[warp * RPW + r] = incl;
+    }
+    __syncwarp();
+    A E[RPW];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) E[r] = s_tr[warp][r][lane];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) s_colp[warp][c * 32 + lane] = colp[c];
+    __syncthreads(); // every thread has read stage st: the producer may refill it
+
+    // ---- phase B: look-backs --------------------------------------------------
+    const bool pub_row = REV ? (tx > 0) : (tx < ntx - 1);
+    const bool pub_col = REV ? (ty > 0) : (ty < nty - 1);
+    const bool stall = (t == P.stall_tile);
+    if (tid < TW) {
+      const int j = tid; // column slot
+      A ac = AR::zero();
+#pragma unroll
+      for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colp[w][j]);
+      unsigned long long* mine = P.col_words + ((unsigned long long)t * TW + j) * K;
+      if (pub_col && !stall) publish<A>(mine, ac, tagA);
+      A run = AR::zero();
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        const int w = REV ? NW - 1 - i : i;
+        const A b = s_colp[w][j];
+        s_colp[w][j] = run;
+        run = AR::add(run, b);
+      }
+      const A above = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
+      if (pub_col && !stall) publish<A>(mine, AR::add(above, ac), tagI);
+      s_colabove[j] = above;
+      if (!CORNER_WARP && j == 0) s_corner = resolve<A>(early_c, cb_base, cb_stride, col_steps, tagA, tagI, P, t);
+    } else if (tid < TW + TH) {
+      const int yy = tid - TW; // tile row
+      const A ar = s_rowagg[yy];
+      unsigned long long* mine = P.row_words + ((unsigned long long)t * TH + yy) * K;
+      if (pub_row && !stall) publish<A>(mine, ar, tagA);
+      const A left = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
+      if (pub_row && !stall) publish<A>(mine, AR::add(left, ar), tagI);
+      s_rowleft[yy] = left;
+      __syncwarp();
+      named_sync(3, TH);
+      if (tid < TW + 32) {
+        // inclusive scan of rowleft over the tile's rows, in scan order; u = total
+        constexpr int PER = TH / 32;
+        A loc[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int q = lane * PER + i;
+          loc[i] = s_rowleft[REV ? TH - 1 - q : q];
+          if (i) loc[i] = AR::add(loc[i - 1], loc[i]);
+        }
+        A incl = loc[PER - 1];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const A o = AR::shfl_up(incl, d);
+          if (lane >= d) incl = AR::add(o, incl);
+        }
+        const A ex = AR::shfl_up(incl, 1);
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+          const int q = lane * PER + i;
+          s_RL[REV ? TH - 1 - q : q] = lane ? AR::add(ex, loc[i]) : loc[i];
+        }
+        unsigned long long* cw = P.corner_words + (unsigned long long)t * K;
+        if (lane == 31) {
+          s_u = incl; // u = sum of rowleft over the tile: the corner aggregate
+          if (pub_col && !stall) publish<A>(cw, incl, tagA);
+        }
+        if (CORNER_WARP) {
+          // with the corner warp's result, publish the corner's inclusive value now
+          named_sync(4, 64);
+          if (lane == 31 && pub_col && !stall) publish<A>(cw, AR::add(s_corner, incl), tagI);
+        }
+      }
+      if (tid == PT && SPARE == 0 && producing) {
+        // producer when no thread is spare: after its own row look-back, tile
+        // k+S-1 into the stage the previous tile's store has finished reading
+        const int ps = (st + S - 1) % S;
+        bulk_wait_read_all();
+        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile,
+                                                            s_img, s_tx, s_ty, s_full);
+        if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
+      }
+    } else if (CORNER_WARP && warp == CW) {
+      if (lane == 0) s_corner = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
+      __syncwarp();
+      named_sync(4, 64);
+    } else if (tid == PT) {
+      // producer: tile k+S-1 into the stage the previous tile's store has
+      // finished reading
+      if (producing) {
+        const int ps = (st + S - 1) % S;
+        bulk_wait_read_all();
+        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile,
+                                                            s_img, s_tx, s_ty, s_full);
+        if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
+      }
+    }
+    __syncthreads();
+
+    // ---- phase D: scan with the carries injected, store ------------------------
+    const A corner = s_corner;
+    if (!CORNER_WARP && tid == 0 && pub_col && !stall)
+      publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(corner, s_u), tagI);
+    // SAT row just outside the warp's rows (above it; below it for the reverse)
+    A top[CPT];
+    {
+      const bool has_prev = REV ? (warp < NW - 1) : (warp > 0);
+      const A rl_prev = has_prev ? s_RL[REV ? (warp + 1) * RPW : warp * RPW - 1] : AR::zero();
+      A cp[CPT];
+#pragma unroll
+      for (int i = 0; i < CPT; ++i) {
+        const int c = REV ? CPT - 1 - i : i;
+        cp[c] = AR::add(s_colabove[c * 32 + lane], s_colp[warp][c * 32 + lane]);
+        if (i) cp[c] = AR::add(cp[REV ? c + 1 : c - 1], cp[c]);
+      }
+      A incl = cp[REV ? 0 : CPT - 1];
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
-        A o[RPW];
-#pragma unroll
-        for (int r = 0; r < RPW; ++r) o[r] = REV ? AR::shfl_down(incl[r], d) : AR::shfl_up(incl[r], d);
-        if (REV ? (lane + d < 32) : (lane >= d)) {
-#pragma unroll
-          for (int r = 0; r < RPW; ++r) incl[r] = AR::add(o[r], incl[r]);
-        }
+        const A o = REV ? AR::shfl_down(incl, d) : AR::shfl_up(incl, d);
+        if (REV ? (lane + d < 32) : (lane >= d)) incl = AR::add(o, incl);
       }
+      A ex = REV ? AR::shfl_down(incl, 1) : AR::shfl_up(incl, 1);
+      if (lane == (REV ? 31 : 0)) ex = AR::zero();
+      const A base = AR::add(AR::add(corner, rl_prev), ex);
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) {
-        const A ex = REV ? AR::shfl_down(incl[r], 1) : AR::shfl_up(incl[r], 1);
-        if (lane != (REV ? 31 : 0)) {
-#pragma unroll
-          for (int c = 0; c < CPT; ++c) v[r][c] = AR::add(ex, v[r][c]);
-        }
-        if (lane == (REV ? 0 : 31)) s_rowagg[buf][warp * RPW + r] = incl[r];
-      }
-#pragma unroll
-      for (int i = 1; i < RPW; ++i) {
-        const int r = REV ? RPW - 1 - i : i;
-        const int p = REV ? r + 1 : r - 1;
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) v[r][c] = AR::add(v[p][c], v[r][c]);
-      }
-#pragma unroll
-      for (int c = 0; c < CPT; ++c) {
-        s_bot[buf][warp][c * 32 + lane] = v[REV ? 0 : RPW - 1][c];
-        s_colraw[buf][warp][c * 32 + lane] = colraw[c];
-      }
-      __syncthreads(); // stage st has been read by every thread: the producer may refill it
-
-      // ---- phases B+C: look-backs (column group | row group), vector scans ------
-      const bool pub_row = REV ? (tx > 0) : (tx < ntx - 1);
-      const bool pub_col = REV ? (ty > 0) : (ty < nty - 1);
-      const bool stall = (t == P.stall_tile);
-      if (tid == PT && TW + TH < NC) {
-        // producer: tile k+S into the stage just read; fetch the ticket after it
-        if (producing) {
-          producing = produce<TIn, REV, TW, TH, SH::STAGE_BYTES>(P, pending, st, stages + st * STAGE_ELEMS, s_tile,
-                                                                 s_img, s_tx, s_ty, s_full);
-          if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
-        }
-      } else if (CT != 0 && tid == CT) {
-        // corner look-back over the tiles above (scalar)
-        s_corner = resolve<A>(early_c, cb_base, cb_stride, col_steps, tagA, tagI, P, t);
-      } else if (tid < TW) {
-        const int j = tid; // column slot
-        A ac = AR::zero();
-#pragma unroll
-        for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colraw[buf][w][j]);
-        unsigned long long* mine = P.col_words + ((unsigned long long)t * TW + j) * K;
-        if (pub_col && !stall) publish<A>(mine, ac, tagA);
-        A run = AR::zero();
-#pragma unroll
-        for (int i = 0; i < NW; ++i) {
-          const int w = REV ? NW - 1 - i : i;
-          const A b = s_bot[buf][w][j];
-          s_bot[buf][w][j] = run;
-          run = AR::add(run, b);
-        }
-        const A above = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
-        if (pub_col && !stall) publish<A>(mine, AR::add(above, ac), tagI);
-        s_colabove[j] = above;
-        if (CT == 0 && j == 0) s_corner = resolve<A>(early_c, cb_base, cb_stride, col_steps, tagA, tagI, P, t);
-        named_sync(2, TW);
-        if (tid < 32) {
-          // inclusive scan of colabove over the tile's columns, in scan order
-          A loc[CPT];
-#pragma unroll
-          for (int i = 0; i < CPT; ++i) {
-            const int slot = REV ? (CPT - 1 - i) * 32 + (31 - lane) : i * 32 + lane;
-            loc[i] = s_colabove[slot];
-            if (i) loc[i] = AR::add(loc[i - 1], loc[i]);
-          }
-          A incl = loc[CPT - 1];
-#pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            const A o = AR::shfl_up(incl, d);
-            if (lane >= d) incl = AR::add(o, incl);
-          }
-          const A ex = AR::shfl_up(incl, 1);
-#pragma unroll
-          for (int i = 0; i < CPT; ++i) {
-            const int slot = REV ? (CPT - 1 - i) * 32 + (31 - lane) : i * 32 + lane;
-            s_CA[slot] = lane ? AR::add(ex, loc[i]) : loc[i];
-          }
-        }
-      } else if (tid < TW + TH) {
-        const int yy = tid - TW; // tile row
-        const A ar = s_rowagg[buf][yy];
-        unsigned long long* mine = P.row_words + ((unsigned long long)t * TH + yy) * K;
-        if (pub_row && !stall) publish<A>(mine, ar, tagA);
-        const A left = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
-        if (pub_row && !stall) publish<A>(mine, AR::add(left, ar), tagI);
-        s_rowleft[yy] = left;
-        named_sync(3, TH);
-        if (tid < TW + 32) {
-          // inclusive scan of rowleft over the tile's rows, in scan order; u = total
-          constexpr int PER = TH / 32;
-          A loc[PER];
-#pragma unroll
-          for (int i = 0; i < PER; ++i) {
-            const int q = lane * PER + i;
-            loc[i] = s_rowleft[REV ? TH - 1 - q : q];
-            if (i) loc[i] = AR::add(loc[i - 1], loc[i]);
-          }
-          A incl = loc[PER - 1];
-#pragma unroll
-          for (int d = 1; d < 32; d <<= 1) {
-            const A o = AR::shfl_up(incl, d);
-            if (lane >= d) incl = AR::add(o, incl);
-          }
-          const A ex = AR::shfl_up(incl, 1);
-#pragma unroll
-          for (int i = 0; i < PER; ++i) {
-            const int q = lane * PER + i;
-            s_RL[REV ? TH - 1 - q : q] = lane ? AR::add(ex, loc[i]) : loc[i];
-          }
-          if (lane == 31) {
-            s_u = incl; // u = sum of rowleft over the tile: the corner aggregate
-            if (pub_col && !stall) publish<A>(P.corner_words + (unsigned long long)t * K, incl, tagA);
-          }
-        }
-        if (tid == PT && TW + TH == NC && producing) {
-          // producer when no thread is idle: after its own row look-back
-          producing = produce<TIn, REV, TW, TH, SH::STAGE_BYTES>(P, pending, st, stages + st * STAGE_ELEMS, s_tile,
-                                                                 s_img, s_tx, s_ty, s_full);
-          if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
-        }
-      }
-      __syncthreads();
-
-      // ---- phase D: add the carries and store ---------------------------------
-      const A corner = s_corner;
-      if (tid == 0 && pub_col && !stall)
-        publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(corner, s_u), tagI);
-      A colterm[CPT];
-#pragma unroll
-      for (int c = 0; c < CPT; ++c)
-        colterm[c] = AR::add(AR::add(s_bot[buf][warp][c * 32 + lane], s_CA[c * 32 + lane]), corner);
-      TOut* out = static_cast<TOut*>(Dp->out) + (y0 + warp * RPW) * out_pitch + xt;
+      for (int c = 0; c < CPT; ++c) top[c] = AR::add(base, cp[c]);
+    }
+    const bool tma_out = flags & kOutTma;
+    {
+      const int64_t out_pitch = Dp.out_pitch;
+      const int64_t height = Dp.height;
       const bool vout = (flags & kOutVec) && nvalid == CPT;
+      TOut* out = static_cast<TOut*>(Dp.out) + (y0 + warp * RPW) * out_pitch + xt;
+      // the stage, reused for this thread's results (its inputs are in registers)
+      TOut* so = reinterpret_cast<TOut*>(stages + st * STAGE_ELEMS) + (warp * RPW) * TW + lane * CPT;
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) {
-        const long long y = y0 + warp * RPW + r;
-        if (y < height && nvalid > 0) {
-          const A rt = s_RL[warp * RPW + r];
-          TOut o[CPT];
+      for (int i = 0; i < RPW; ++i) {
+        const int r = REV ? RPW - 1 - i : i;
+        const TIn* x = raw[r].u.e;
+        A run = AR::add(E[r], s_rowleft[warp * RPW + r]);
+        TOut o[CPT];
 #pragma unroll
-          for (int c = 0; c < CPT; ++c) o[c] = OutCvt<TOut, A>::out(AR::add(AR::add(v[r][c], rt), colterm[c]));
-          store_seg<TOut, CPT>(out, vout, nvalid, o);
+        for (int ii = 0; ii < CPT; ++ii) {
+          const int c = REV ? CPT - 1 - ii : ii;
+          run = AR::add(run, Cvt<A, TIn>::in(x[c]));
+          top[c] = AR::add(top[c], run);
+          o[c] = OutCvt<TOut, A>::out(top[c]);
         }
-        out += out_pitch;
+        if (tma_out) {
+          union {
+            uint4 v;
+            TOut e[CPT];
+          } u;
+#pragma unroll
+          for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
+          *reinterpret_cast<uint4*>(so + r * TW) = u.v;
+        } else if (y0 + warp * RPW + r < height && nvalid > 0) {
+          store_seg<TOut, CPT>(out + r * out_pitch, vout, nvalid, o);
+        }
+      }
+    }
+    // end of the tile: shared vectors may be reused, and with TMA output one
+    // bulk tensor store moves the tile out (clipped at the image edges) and
+    // drains while the CTA goes on with the next tile
+    if (tma_out) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tma_out) {
+      if (tid == PT) {
+        const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[img].tmap_out;
+        tma_store_2d(map, tx * TW, ty * TH, smem_u32(stages + st * STAGE_ELEMS));
       }
     }
   }
+  if (tid == PT) bulk_wait_all(); // stores read shared memory until they complete
 
   // ---- end of launch: the last CTA resets the ticket and advances the epoch --
   __syncthreads();

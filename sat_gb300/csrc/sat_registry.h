@@ -27,12 +27,13 @@ struct Variant {
   int TH, TW, K, threads, dyn_smem;
 };
 
-// Tile configurations (rows per consumer warp; 8 consumer warps each).
+// Tile configurations (rows per warp, warps per CTA).
 struct TileConfig {
   int rows_per_warp;
+  int warps;
   const char* name;
 };
-constexpr int kNumConfigs = 3;
+constexpr int kNumConfigs = 4;
 extern const TileConfig kConfigs[kNumConfigs];
 
 // Lists of variants, one per instantiation translation unit.

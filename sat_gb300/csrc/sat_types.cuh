@@ -34,8 +34,8 @@ struct Ar<uint32_t> {
   static constexpr int K = 1;
   __device__ __forceinline__ static uint32_t zero() { return 0u; }
   __device__ __forceinline__ static uint32_t add(uint32_t a, uint32_t b) { return a + b; }
-  __device__ __forceinline__ static uint32_t shfl_up(uint32_t a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
-  __device__ __forceinline__ static uint32_t shfl_down(uint32_t a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static uint32_t shfl_up(uint32_t a, int d, int w = 32) { return __shfl_up_sync(0xffffffffu, a, d, w); }
+  __device__ __forceinline__ static uint32_t shfl_down(uint32_t a, int d, int w = 32) { return __shfl_down_sync(0xffffffffu, a, d, w); }
   __device__ __forceinline__ static uint32_t shfl(uint32_t a, int l) { return __shfl_sync(0xffffffffu, a, l); }
   __device__ __forceinline__ static void to_words(uint32_t a, uint32_t* w) { w[0] = a; }
   __device__ __forceinline__ static uint32_t from_words(const uint32_t* w) { return w[0]; }
@@ -46,8 +46,8 @@ struct Ar<float> {
   static constexpr int K = 1;
   __device__ __forceinline__ static float zero() { return 0.f; }
   __device__ __forceinline__ static float add(float a, float b) { return __fadd_rn(a, b); }
-  __device__ __forceinline__ static float shfl_up(float a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
-  __device__ __forceinline__ static float shfl_down(float a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static float shfl_up(float a, int d, int w = 32) { return __shfl_up_sync(0xffffffffu, a, d, w); }
+  __device__ __forceinline__ static float shfl_down(float a, int d, int w = 32) { return __shfl_down_sync(0xffffffffu, a, d, w); }
   __device__ __forceinline__ static float shfl(float a, int l) { return __shfl_sync(0xffffffffu, a, l); }
   __device__ __forceinline__ static void to_words(float a, uint32_t* w) { w[0] = __float_as_uint(a); }
   __device__ __forceinline__ static float from_words(const uint32_t* w) { return __uint_as_float(w[0]); }
@@ -58,8 +58,8 @@ struct Ar<double> {
   static constexpr int K = 2;
   __device__ __forceinline__ static double zero() { return 0.0; }
   __device__ __forceinline__ static double add(double a, double b) { return __dadd_rn(a, b); }
-  __device__ __forceinline__ static double shfl_up(double a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
-  __device__ __forceinline__ static double shfl_down(double a, int d) { return __shfl_down_sync(0xffffffffu, a, d); }
+  __device__ __forceinline__ static double shfl_up(double a, int d, int w = 32) { return __shfl_up_sync(0xffffffffu, a, d, w); }
+  __device__ __forceinline__ static double shfl_down(double a, int d, int w = 32) { return __shfl_down_sync(0xffffffffu, a, d, w); }
   __device__ __forceinline__ static double shfl(double a, int l) { return __shfl_sync(0xffffffffu, a, l); }
   __device__ __forceinline__ static void to_words(double a, uint32_t* w) {
     unsigned long long b = (unsigned long long)__double_as_longlong(a);
@@ -80,11 +80,11 @@ struct Ar<CF32> {
     float s = two_sum(a.s, b.s, err);
     return CF32{s, __fadd_rn(__fadd_rn(a.e, b.e), err)};
   }
-  __device__ __forceinline__ static CF32 shfl_up(CF32 a, int d) {
-    return CF32{__shfl_up_sync(0xffffffffu, a.s, d), __shfl_up_sync(0xffffffffu, a.e, d)};
+  __device__ __forceinline__ static CF32 shfl_up(CF32 a, int d, int w = 32) {
+    return CF32{__shfl_up_sync(0xffffffffu, a.s, d, w), __shfl_up_sync(0xffffffffu, a.e, d, w)};
   }
-  __device__ __forceinline__ static CF32 shfl_down(CF32 a, int d) {
-    return CF32{__shfl_down_sync(0xffffffffu, a.s, d), __shfl_down_sync(0xffffffffu, a.e, d)};
+  __device__ __forceinline__ static CF32 shfl_down(CF32 a, int d, int w = 32) {
+    return CF32{__shfl_down_sync(0xffffffffu, a.s, d, w), __shfl_down_sync(0xffffffffu, a.e, d, w)};
   }
   __device__ __forceinline__ static CF32 shfl(CF32 a, int l) {
     return CF32{__shfl_sync(0xffffffffu, a.s, l), __shfl_sync(0xffffffffu, a.e, l)};

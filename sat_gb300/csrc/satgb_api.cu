@@ -26,9 +26,10 @@
 namespace satgb {
 
 const TileConfig kConfigs[kNumConfigs] = {
-    {8, "64-row tiles (8 rows per warp)"},
-    {16, "128-row tiles (16 rows per warp)"},
-    {4, "32-row tiles (4 rows per warp)"},
+    {8, 8, "64-row tiles, 8 warps"},
+    {16, 8, "128-row tiles, 8 warps"},
+    {4, 8, "32-row tiles, 8 warps"},
+    {8, 16, "128-row tiles, 16 warps"},
 };
 
 namespace {
@@ -75,9 +76,12 @@ void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const 
   uint32_t flags = 0;
   if (((uintptr_t)in % seg_in) == 0 && ((size_t)in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
   if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0) flags |= kOutVec;
-  // TMA: 16-byte aligned base and row pitch, extents within 2^32
-  if (((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * in_sz) % 16 == 0 && width < (1LL << 32) &&
-      height < (1LL << 32)) {
+  // TMA moves whole 16-byte chunks of a row, so it is used only when the
+  // base, the row pitch and the row's length are all multiples of 16 bytes:
+  // then no chunk reaches into a row's padding or past the buffer.
+  // Other images use plain loads and stores.
+  if (((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * in_sz) % 16 == 0 && ((size_t)width * in_sz) % 16 == 0 &&
+      width < (1LL << 32) && height < (1LL << 32)) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
     if (enc) {
       CUtensorMapDataType dt = in_sz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
@@ -93,6 +97,24 @@ void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const 
                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
       if (r == CUDA_SUCCESS) flags |= kInTma;
+    }
+  }
+  if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0 && ((size_t)width * out_sz) % 16 == 0 &&
+      width < (1LL << 32) && height < (1LL << 32)) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (enc) {
+      CUtensorMapDataType dt = out_t == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                               : out_t == 5 ? CU_TENSOR_MAP_DATA_TYPE_INT32
+                               : out_t == 6 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+      cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+      cuuint64_t strides[1] = {(cuuint64_t)(out_pitch * (int64_t)out_sz)};
+      cuuint32_t box[2] = {(cuuint32_t)v->TW, (cuuint32_t)v->TH};
+      cuuint32_t estr[2] = {1, 1};
+      CUresult r = enc(&d.tmap_out, dt, 2, out, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r == CUDA_SUCCESS) flags |= kOutTma;
     }
   }
   d.flags = flags;
