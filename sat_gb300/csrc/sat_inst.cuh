@@ -53,18 +53,20 @@ Variant make_variant(int in_t, int out_t, int mode, int cfg) {
 #define SG_F32 6
 #define SG_F64 7
 
-// every tile configuration, both directions:
-//   0: 64-row tiles, 8 warps, 2 CTAs/SM     1: 128-row tiles, 8 warps
-//   2: 32-row tiles, 8 warps                3: 128-row tiles, 16 warps, 1 CTA/SM
-#define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                    \
-  satgb::make_variant<TIN, TOUT, A, false, 8, 8, 2>(IT, OT, MODE, 0),         \
-      satgb::make_variant<TIN, TOUT, A, false, 16, 8, 1>(IT, OT, MODE, 1),    \
-      satgb::make_variant<TIN, TOUT, A, false, 4, 8, 2>(IT, OT, MODE, 2),     \
-      satgb::make_variant<TIN, TOUT, A, false, 8, 16, 1>(IT, OT, MODE, 3),    \
-      satgb::make_variant<TIN, TOUT, A, true, 8, 8, 2>(IT, OT, MODE, 0),      \
-      satgb::make_variant<TIN, TOUT, A, true, 16, 8, 1>(IT, OT, MODE, 1),     \
-      satgb::make_variant<TIN, TOUT, A, true, 4, 8, 2>(IT, OT, MODE, 2),      \
-      satgb::make_variant<TIN, TOUT, A, true, 8, 16, 1>(IT, OT, MODE, 3)
+// every tile configuration, both directions (rows per warp, warps, CTAs per SM):
+//   0: 64-row tiles, 16 warps       1: 128-row tiles, 16 warps (64-row for
+//                                       8-byte accumulators: shared memory)
+//   2: 32-row tiles, 8 warps, 2 CTAs per SM     3: 32-row tiles, 16 warps
+#define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
+#define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                            \
+  satgb::make_variant<TIN, TOUT, A, false, 4, 16, 1>(IT, OT, MODE, 0),                \
+      satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1), \
+      satgb::make_variant<TIN, TOUT, A, false, 4, 8, 2>(IT, OT, MODE, 2),             \
+      satgb::make_variant<TIN, TOUT, A, false, 2, 16, 1>(IT, OT, MODE, 3),            \
+      satgb::make_variant<TIN, TOUT, A, true, 4, 16, 1>(IT, OT, MODE, 0),             \
+      satgb::make_variant<TIN, TOUT, A, true, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),  \
+      satgb::make_variant<TIN, TOUT, A, true, 4, 8, 2>(IT, OT, MODE, 2),              \
+      satgb::make_variant<TIN, TOUT, A, true, 2, 16, 1>(IT, OT, MODE, 3)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

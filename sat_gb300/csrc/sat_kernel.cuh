@@ -96,7 +96,7 @@ struct SatParams {
 // (CTAS CTAs per SM) next to its static shared memory, between 2 and 6.
 template <int STAGE_BYTES, int STATIC_BYTES, int CTAS>
 struct Stages {
-  static constexpr int budget = (CTAS == 1 ? 227 * 1024 : 113 * 1024) - STATIC_BYTES - 1024;
+  static constexpr int budget = (CTAS == 1 ? 232448 : 115712) - STATIC_BYTES; // per-CTA limit, 1 or 2 CTAs per SM
   static constexpr int fit = budget / STAGE_BYTES;
   static constexpr int value = fit < 2 ? 2 : (fit > 6 ? 6 : fit);
 };
@@ -217,6 +217,25 @@ __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bu
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Shared-memory loads and stores the compiler may not cache or reorder
+// (values handed between warps without a barrier).
+template <class T>
+__device__ __forceinline__ T vload(const T* p) {
+  T r;
+  const volatile uint32_t* src = reinterpret_cast<const volatile uint32_t*>(p);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 4); ++i) dst[i] = src[i];
+  return r;
+}
+template <class T>
+__device__ __forceinline__ void vstore(T* p, const T& v) {
+  volatile uint32_t* dst = reinterpret_cast<volatile uint32_t*>(p);
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(&v);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 4); ++i) dst[i] = src[i];
 }
 
 // Records a device error (first one wins) in the workspace header.
@@ -422,7 +441,7 @@ struct TileShape {
   static constexpr int IN_BYTES = TH * TW * (int)sizeof(TIn); // what the TMA load brings
   static constexpr int STAGE_BYTES = TH * TW * (int)(sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
   // static shared memory of the kernel (s_tr, s_colp, the vectors), roughly
-  static constexpr int STATIC_BYTES = (NW * RPW * 33 + NW * TW + 3 * TH + TW) * (int)sizeof(A) + 256;
+  static constexpr int STATIC_BYTES = (NW * RPW * 32 + 2 * NW * TW + 3 * TH + TW) * (int)sizeof(A) + 512;
   static constexpr int S = Stages<STAGE_BYTES, STATIC_BYTES, CTAS>::value;
   static constexpr int DYN_SMEM = S * STAGE_BYTES;
   static constexpr int THREADS = NW * 32;
@@ -470,25 +489,29 @@ __device__ __forceinline__ bool produce(const SatParams& P, unsigned long long t
 }
 
 // ---------------------------------------------------------------------------
-// The tile kernel.  Per tile, with the tile resident in a shared-memory stage:
+// The tile kernel.  Tiles are software-pipelined through the CTA: iteration k
+// runs the local phase of tile k+1, then the look-back of tile k, then the
+// output phase of tile k, so the round trips of tile k's look-back overlap
+// tile k+1's local work.
 //
-//  A  aggregates: each thread sums its CPT-column x RPW-row block by columns
-//     (colp) and by rows (rowp).  A transpose through shared memory turns the
-//     32 lanes' row partials of each row into the exclusive prefix E over the
-//     lanes (kept in registers) and the row total (the tile's row aggregate).
-//     Column partials go to shared memory.  Then one barrier.
-//  B  look-backs: threads [0,TW) sum the column partials into the tile's
-//     column aggregate (published), turn them into the exclusive prefix over
-//     warps C_w, and look back up the column; threads [TW,TW+TH) publish the
-//     row aggregate and look back along the row; a spare warp looks back over
-//     the corner words; a spare thread takes the next ticket and starts the
-//     next tile's TMA load.  The row group then scans rowleft over the rows
-//     (RL) and computes u = sum rowleft; with the corner known the corner's
-//     inclusive value is published right away.
-//  D  scan + store: warp w forms the SAT row just above its rows,
+//  A  (tile k+1) aggregates: each thread sums its CPT-column x RPW-row block by
+//     columns (colp) and by rows (rowp).  A transpose through shared memory
+//     turns the 32 lanes' row partials of each row into the exclusive prefix E
+//     over the lanes (kept in registers until the output phase) and the row
+//     total.  Column partials and row totals go to shared memory.
+//  B  threads [0,TW): sum tile k+1's column partials into its column
+//     aggregate (published at once) and turn them into the exclusive prefix
+//     over warps C_w; then finish tile k's column look-back and publish its
+//     inclusive column sums.  Threads [TW,TW+TH) do the same for rows, then
+//     scan tile k's rowleft over its rows (RL) and form u = sum rowleft, the
+//     corner aggregate.  A spare warp resolves tile k's corner (so the
+//     corner's inclusive value corner + u is published right away); a spare
+//     thread takes tickets and starts TMA loads.
+//  D  (tile k) output: warp w forms the SAT row just above its rows,
 //        Top_w(x) = corner + RL(above the warp) + sum_{x0<=i<=x} (colabove(i) + C_w(i)),
-//     then walks its rows once: run = rowleft(y) + E(y) + in-thread row prefix,
-//     acc(x) += run, and stores acc.  About four additions per element.
+//     then walks its rows once: run = rowleft(y) + E(y) + in-thread row
+//     prefix, acc(x) += run.  Results go back into the tile's stage and leave
+//     by one TMA store (or by plain stores for images TMA cannot address).
 //
 // The reverse (suffix) SAT runs every scan in the opposite direction.
 // ---------------------------------------------------------------------------
@@ -502,27 +525,31 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   constexpr int NC = NW * 32;
   constexpr int STAGE_ELEMS = SH::STAGE_BYTES / (int)sizeof(TIn); // stage stride in input elements
   constexpr int SPARE = NC - (TW + TH);
-  static_assert(SPARE >= 0, "one thread per row and per column of the tile");
+  static_assert(SPARE >= 64, "threads for rows, columns, the corner warp and the producer");
   static_assert(TH % 32 == 0 && TW % 32 == 0, "groups are whole warps");
   static_assert(32 % RPW == 0, "rows per warp divide the warp");
-  constexpr bool CORNER_WARP = SPARE >= 64; // a spare warp for the corner, another one holds the producer
-  constexpr int CW = (TW + TH) / 32;        // that corner warp
-  constexpr int PT = NC - 1;                // producer thread
-  constexpr int LPR = 32 / RPW;             // transpose-scan: lanes per row ...
-  constexpr int CH = RPW;                   // ... and values per lane
+  static_assert(S >= 3, "a stage for the tile in output, one in the local phase, one loading");
+  constexpr int CW = (TW + TH) / 32; // corner warp
+  constexpr int PT = NC - 1;         // producer thread (in the last warp, never the corner warp)
+  static_assert(CW < NW - 1, "corner warp and producer warp differ");
+  constexpr int LPR = 32 / RPW;      // transpose-scan: lanes per row ...
+  constexpr int CH = RPW;            // ... and values per lane
   constexpr int K = Ar<A>::K;
+  constexpr bool WIDEN = sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
   using AR = Ar<A>;
 
   extern __shared__ __align__(128) unsigned char dsmem[];
   TIn* stages = reinterpret_cast<TIn*>(dsmem);
 
-  __shared__ A s_tr[NW][RPW][33];   // per-warp transpose scratch for the row offsets
-  __shared__ A s_colp[NW][TW];      // per warp: raw column partials (by slot); then the exclusive prefix over warps
-  __shared__ A s_rowagg[TH];        // row totals of the tile
-  __shared__ A s_rowleft[TH];       // row look-back result
-  __shared__ A s_RL[TH];            // scan of rowleft over the tile's rows
-  __shared__ A s_colabove[TW];      // column look-back result (by slot)
+  __shared__ A s_tr[NW][RPW][32];   // per-warp transpose scratch (index lane ^ row: conflict free)
+  __shared__ A s_colp[2][NW][TW];   // per warp: raw column partials (by slot); then the exclusive prefix over warps
+  __shared__ A s_rowagg[TH];        // row totals of the tile in the local phase
+  __shared__ A s_rowleft[TH];       // row look-back result of the tile in the output phase
+  __shared__ A s_RL[TH];            // its scan over each 32-row group of the tile's rows
+  __shared__ A s_rlw[TH / 32];      // per 32-row group: the sum of rowleft
+  __shared__ A s_colabove[TW];      // its column look-back result (by slot)
   __shared__ A s_corner, s_u;
+  __shared__ int s_cnt_row, s_cnt_corner; // arrivals of the row warps / of {rows, corner}
   __shared__ long long s_tile[S];   // spatial tile index per stage (-1: no more tiles)
   __shared__ int s_img[S];
   __shared__ int s_tx[S], s_ty[S];
@@ -537,6 +564,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 
   unsigned long long pending = 0; // producer thread: the next ticket, fetched a tile ahead
   bool producing = true;
+  if (tid == 0) {
+    s_cnt_row = 0;
+    s_cnt_corner = 0;
+  }
   if (tid == PT) {
 #pragma unroll
     for (int s = 0; s < S; ++s) mbar_init(smem_u32(&s_full[s]), 1);
@@ -545,96 +576,82 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     for (int s = 0; s < S - 1; ++s) {
       if (producing)
         producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, atomicAdd(&P.ws->ticket, 1ull), s,
-                                                               stages + s * STAGE_ELEMS, s_tile, s_img, s_tx,
-                                                               s_ty, s_full);
+                                                            stages + s * STAGE_ELEMS, s_tile, s_img, s_tx, s_ty,
+                                                            s_full);
     }
     if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
   }
   __syncthreads();
 
-  for (int k = 0;; ++k) {
-    const int st = k % S;
-    mbar_wait_bounded(smem_u32(&s_full[st]), (k / S) & 1, P, -1);
-    const long long t = s_tile[st];
-    if (t < 0) break;
-    const int tx = s_tx[st], ty = s_ty[st];
-    const int img = s_img[st];
-    const ImageView Dp = image_view(P, img);
-    const int ntx = Dp.ntx, nty = Dp.nty;
-    const uint32_t flags = Dp.flags;
-    const long long x0 = (long long)tx * TW;
-    const long long y0 = (long long)ty * TH;
+  // ---- per-tile state carried from the local phase to the output phase ---------
+  struct Tile {
+    long long t;
+    int tx, ty, img;
+  };
+  Tile nxt, cur;
+  A E_nxt[RPW], E_cur[RPW];
+  A agg_cur = AR::zero(); // this thread's element of the current tile's aggregate (column or row groups)
+  EarlyWin<A> win;        // look-back window of the current tile (columns, rows or the corner)
+  const unsigned long long* lb_base = nullptr;
+  long long lb_stride = 0;
+  int lb_steps = 0;
+
+  // phase A for the tile in stage kk % S; false when the tickets ran out
+  auto phase_a = [&](int kk) -> bool {
+    const int st = kk % S;
+    mbar_wait_bounded(smem_u32(&s_full[st]), (kk / S) & 1, P, -1);
+    nxt.t = s_tile[st];
+    if (nxt.t < 0) return false;
+    nxt.tx = s_tx[st];
+    nxt.ty = s_ty[st];
+    nxt.img = s_img[st];
+    const ImageView D = image_view(P, nxt.img);
+    const uint32_t flags = D.flags;
+    const long long x0 = (long long)nxt.tx * TW, y0 = (long long)nxt.ty * TH;
     const long long xt = x0 + (long long)lane * CPT;
-    const long long rem = Dp.width - xt;
+    const long long rem = D.width - xt;
     const int nvalid = rem <= 0 ? 0 : (rem >= CPT ? CPT : (int)rem);
-    TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT; // this thread's block in the stage
-
-    // early look-back reads: the W nearest predecessors of this thread's element
-    const int col_steps = REV ? (nty - 1 - ty) : ty;
-    const int row_steps = REV ? (ntx - 1 - tx) : tx;
-    EarlyWin<A> early;
-    const unsigned long long* lb_base = nullptr;
-    long long lb_stride = 0;
-    int lb_steps = 0;
-    if (tid < TW) {
-      lb_base = P.col_words + ((unsigned long long)t * TW + tid) * K;
-      lb_stride = (REV ? 1 : -1) * (long long)ntx * TW * K;
-      lb_steps = col_steps;
-    } else if (tid < TW + TH) {
-      lb_base = P.row_words + ((unsigned long long)t * TH + (tid - TW)) * K;
-      lb_stride = (REV ? 1 : -1) * (long long)TH * K;
-      lb_steps = row_steps;
-    } else if ((CORNER_WARP && warp == CW && lane == 0) || (!CORNER_WARP && tid == 0)) {
-      lb_base = P.corner_words + (unsigned long long)t * K;
-      lb_stride = (REV ? 1 : -1) * (long long)ntx * K;
-      lb_steps = col_steps;
-    }
-    EarlyWin<A> early_c; // thread 0's corner window when there is no corner warp
-    if (lb_base) early_read<A>(early, lb_base, lb_stride, lb_steps);
-    const unsigned long long* cb_base = P.corner_words + (unsigned long long)t * K;
-    const long long cb_stride = (REV ? 1 : -1) * (long long)ntx * K;
-    if (!CORNER_WARP && tid == 0) early_read<A>(early_c, cb_base, cb_stride, col_steps);
-
-    // ---- phase A: aggregates --------------------------------------------------
-    // the thread's block stays in registers (packed) until phase D, so the
-    // stage is free for the next tile's TMA as soon as phase A ends
-    RowSeg<TIn, CPT> raw[RPW];
+    TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
     A colp[CPT], rowp[RPW];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) colp[c] = AR::zero();
-    {
-      const bool tma = flags & kInTma;
-      const TIn* gin = static_cast<const TIn*>(Dp.in) + (y0 + warp * RPW) * Dp.in_pitch + xt;
-      const bool vin = (flags & kInVec) && nvalid == CPT;
+    const bool tma = flags & kInTma;
+    const TIn* gin = static_cast<const TIn*>(D.in) + (y0 + warp * RPW) * D.in_pitch + xt;
+    const bool vin = (flags & kInVec) && nvalid == CPT;
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) {
-        if (tma) {
-          raw[r].u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
-        } else if (y0 + warp * RPW + r < Dp.height && nvalid > 0) {
-          load_seg<TIn, CPT>(gin + r * Dp.in_pitch, vin, nvalid, raw[r].u.e);
+    for (int r = 0; r < RPW; ++r) {
+      RowSeg<TIn, CPT> x;
+      if (tma) {
+        x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+      } else {
+        // no TMA for this image: load from global memory and park the values in
+        // the stage for the output phase (each thread reads back only its own block)
+        if (y0 + warp * RPW + r < D.height && nvalid > 0) {
+          load_seg<TIn, CPT>(gin + r * D.in_pitch, vin, nvalid, x.u.e);
         } else {
 #pragma unroll
-          for (int c = 0; c < CPT; ++c) raw[r].u.e[c] = TIn(0);
+          for (int c = 0; c < CPT; ++c) x.u.e[c] = TIn(0);
         }
-        A rs = AR::zero();
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-          const A a = Cvt<A, TIn>::in(raw[r].u.e[c]);
-          colp[c] = AR::add(colp[c], a);
-          rs = AR::add(rs, a);
-        }
-        rowp[r] = rs;
+        *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = x.u.v;
       }
+      A rs = AR::zero();
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const A a = Cvt<A, TIn>::in(x.u.e[c]);
+        colp[c] = AR::add(colp[c], a);
+        rs = AR::add(rs, a);
+      }
+      rowp[r] = rs;
     }
     // row partials -> exclusive prefix over the lanes (E) and the row totals
 #pragma unroll
-    for (int r = 0; r < RPW; ++r) s_tr[warp][r][lane] = rowp[r];
+    for (int r = 0; r < RPW; ++r) s_tr[warp][r][lane ^ r] = rowp[r];
     __syncwarp();
     {
       const int r = lane / LPR, q = lane % LPR;
       A tot = AR::zero();
 #pragma unroll
-      for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][q * CH + (REV ? CH - 1 - i : i)]);
+      for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][(q * CH + (REV ? CH - 1 - i : i)) ^ r]);
       A incl = tot;
 #pragma unroll
       for (int d = 1; d < LPR; d <<= 1) {
@@ -645,7 +662,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
 #pragma unroll
       for (int i = 0; i < CH; ++i) {
-        const int idx = q * CH + (REV ? CH - 1 - i : i);
+        const int idx = (q * CH + (REV ? CH - 1 - i : i)) ^ r;
         const A vv = s_tr[warp][r][idx];
         s_tr[warp][r][idx] = ex;
         ex = AR::add(ex, vv);
@@ -653,151 +670,217 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       if (q == (REV ? 0 : LPR - 1)) s_rowagg[warp * RPW + r] = incl;
     }
     __syncwarp();
-    A E[RPW];
 #pragma unroll
-    for (int r = 0; r < RPW; ++r) E[r] = s_tr[warp][r][lane];
+    for (int r = 0; r < RPW; ++r) E_nxt[r] = s_tr[warp][r][lane ^ r];
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) s_colp[warp][c * 32 + lane] = colp[c];
-    __syncthreads(); // every thread has read stage st: the producer may refill it
+    for (int c = 0; c < CPT; ++c) s_colp[kk & 1][warp][c * 32 + lane] = colp[c];
+    if (!tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    return true;
+  };
 
-    // ---- phase B: look-backs --------------------------------------------------
-    const bool pub_row = REV ? (tx > 0) : (tx < ntx - 1);
-    const bool pub_col = REV ? (ty > 0) : (ty < nty - 1);
+  // publish the new tile's aggregate (column or row element), start its look-back window
+  auto start_lookback = [&](int kk) {
+    const long long t = nxt.t;
+    const ImageView D = image_view(P, nxt.img);
+    const int ntx = D.ntx, nty = D.nty;
     const bool stall = (t == P.stall_tile);
     if (tid < TW) {
-      const int j = tid; // column slot
+      const int j = tid;
       A ac = AR::zero();
 #pragma unroll
-      for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colp[w][j]);
-      unsigned long long* mine = P.col_words + ((unsigned long long)t * TW + j) * K;
-      if (pub_col && !stall) publish<A>(mine, ac, tagA);
+      for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colp[kk & 1][w][j]);
+      if ((REV ? (nxt.ty > 0) : (nxt.ty < nty - 1)) && !stall)
+        publish<A>(P.col_words + ((unsigned long long)t * TW + j) * K, ac, tagA);
       A run = AR::zero();
 #pragma unroll
       for (int i = 0; i < NW; ++i) {
         const int w = REV ? NW - 1 - i : i;
-        const A b = s_colp[w][j];
-        s_colp[w][j] = run;
+        const A b = s_colp[kk & 1][w][j];
+        s_colp[kk & 1][w][j] = run;
         run = AR::add(run, b);
       }
-      const A above = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
-      if (pub_col && !stall) publish<A>(mine, AR::add(above, ac), tagI);
-      s_colabove[j] = above;
-      if (!CORNER_WARP && j == 0) s_corner = resolve<A>(early_c, cb_base, cb_stride, col_steps, tagA, tagI, P, t);
+      agg_cur = ac;
+      lb_base = P.col_words + ((unsigned long long)t * TW + j) * K;
+      lb_stride = (REV ? 1 : -1) * (long long)ntx * TW * K;
+      lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
+      early_read<A>(win, lb_base, lb_stride, lb_steps);
     } else if (tid < TW + TH) {
-      const int yy = tid - TW; // tile row
+      const int yy = tid - TW;
       const A ar = s_rowagg[yy];
-      unsigned long long* mine = P.row_words + ((unsigned long long)t * TH + yy) * K;
-      if (pub_row && !stall) publish<A>(mine, ar, tagA);
-      const A left = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
-      if (pub_row && !stall) publish<A>(mine, AR::add(left, ar), tagI);
-      s_rowleft[yy] = left;
-      __syncwarp();
-      named_sync(3, TH);
-      if (tid < TW + 32) {
-        // inclusive scan of rowleft over the tile's rows, in scan order; u = total
-        constexpr int PER = TH / 32;
-        A loc[PER];
-#pragma unroll
-        for (int i = 0; i < PER; ++i) {
-          const int q = lane * PER + i;
-          loc[i] = s_rowleft[REV ? TH - 1 - q : q];
-          if (i) loc[i] = AR::add(loc[i - 1], loc[i]);
-        }
-        A incl = loc[PER - 1];
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          const A o = AR::shfl_up(incl, d);
-          if (lane >= d) incl = AR::add(o, incl);
-        }
-        const A ex = AR::shfl_up(incl, 1);
-#pragma unroll
-        for (int i = 0; i < PER; ++i) {
-          const int q = lane * PER + i;
-          s_RL[REV ? TH - 1 - q : q] = lane ? AR::add(ex, loc[i]) : loc[i];
-        }
-        unsigned long long* cw = P.corner_words + (unsigned long long)t * K;
-        if (lane == 31) {
-          s_u = incl; // u = sum of rowleft over the tile: the corner aggregate
-          if (pub_col && !stall) publish<A>(cw, incl, tagA);
-        }
-        if (CORNER_WARP) {
-          // with the corner warp's result, publish the corner's inclusive value now
-          named_sync(4, 64);
-          if (lane == 31 && pub_col && !stall) publish<A>(cw, AR::add(s_corner, incl), tagI);
-        }
-      }
-      if (tid == PT && SPARE == 0 && producing) {
-        // producer when no thread is spare: after its own row look-back, tile
-        // k+S-1 into the stage the previous tile's store has finished reading
-        const int ps = (st + S - 1) % S;
-        bulk_wait_read_all();
-        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile,
-                                                            s_img, s_tx, s_ty, s_full);
-        if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
-      }
-    } else if (CORNER_WARP && warp == CW) {
-      if (lane == 0) s_corner = resolve<A>(early, lb_base, lb_stride, lb_steps, tagA, tagI, P, t);
-      __syncwarp();
-      named_sync(4, 64);
-    } else if (tid == PT) {
-      // producer: tile k+S-1 into the stage the previous tile's store has
-      // finished reading
-      if (producing) {
-        const int ps = (st + S - 1) % S;
-        bulk_wait_read_all();
-        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile,
-                                                            s_img, s_tx, s_ty, s_full);
-        if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
-      }
+      if ((REV ? (nxt.tx > 0) : (nxt.tx < ntx - 1)) && !stall)
+        publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, ar, tagA);
+      agg_cur = ar;
+      lb_base = P.row_words + ((unsigned long long)t * TH + yy) * K;
+      lb_stride = (REV ? 1 : -1) * (long long)TH * K;
+      lb_steps = REV ? (ntx - 1 - nxt.tx) : nxt.tx;
+      early_read<A>(win, lb_base, lb_stride, lb_steps);
+    } else if (warp == CW && lane == 0) {
+      lb_base = P.corner_words + (unsigned long long)t * K;
+      lb_stride = (REV ? 1 : -1) * (long long)ntx * K;
+      lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
+      early_read<A>(win, lb_base, lb_stride, lb_steps);
     }
+  };
+
+  bool have = phase_a(0);
+  __syncthreads();
+  if (have) start_lookback(0);
+
+  for (int k = 0; have; ++k) {
+    const int st = k % S;
+    cur = nxt;
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) E_cur[r] = E_nxt[r];
+    const A my_agg = agg_cur;
+    EarlyWin<A> my_win = win;
+    const unsigned long long* my_base = lb_base;
+    const long long my_stride = lb_stride;
+    const int my_steps = lb_steps;
+
+    // ---- A(k+1) ----------------------------------------------------------------
+    const bool have_next = phase_a(k + 1);
     __syncthreads();
 
-    // ---- phase D: scan with the carries injected, store ------------------------
-    const A corner = s_corner;
-    if (!CORNER_WARP && tid == 0 && pub_col && !stall)
-      publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(corner, s_u), tagI);
-    // SAT row just outside the warp's rows (above it; below it for the reverse)
-    A top[CPT];
+    // ---- B: the next tile's aggregates out, the current tile's look-backs in ----
+    const long long t = cur.t;
+    const bool stall = (t == P.stall_tile);
+    bool pub_row, pub_col;
     {
-      const bool has_prev = REV ? (warp < NW - 1) : (warp > 0);
-      const A rl_prev = has_prev ? s_RL[REV ? (warp + 1) * RPW : warp * RPW - 1] : AR::zero();
-      A cp[CPT];
-#pragma unroll
-      for (int i = 0; i < CPT; ++i) {
-        const int c = REV ? CPT - 1 - i : i;
-        cp[c] = AR::add(s_colabove[c * 32 + lane], s_colp[warp][c * 32 + lane]);
-        if (i) cp[c] = AR::add(cp[REV ? c + 1 : c - 1], cp[c]);
-      }
-      A incl = cp[REV ? 0 : CPT - 1];
+      const ImageView D = image_view(P, cur.img);
+      pub_row = REV ? (cur.tx > 0) : (cur.tx < D.ntx - 1);
+      pub_col = REV ? (cur.ty > 0) : (cur.ty < D.nty - 1);
+    }
+    if (have_next) start_lookback(k + 1);
+    if (tid < TW) {
+      const A above = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+      if (pub_col && !stall) publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
+      s_colabove[tid] = above;
+    } else if (tid < TW + TH) {
+      const int yy = tid - TW;
+      const A left = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+      if (pub_row && !stall) publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, AR::add(left, my_agg), tagI);
+      s_rowleft[yy] = left;
+      // scan of rowleft over this warp's 32 rows, in scan order; the group sum
+      A incl = left;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
         const A o = REV ? AR::shfl_down(incl, d) : AR::shfl_up(incl, d);
         if (REV ? (lane + d < 32) : (lane >= d)) incl = AR::add(o, incl);
       }
-      A ex = REV ? AR::shfl_down(incl, 1) : AR::shfl_up(incl, 1);
-      if (lane == (REV ? 31 : 0)) ex = AR::zero();
-      const A base = AR::add(AR::add(corner, rl_prev), ex);
+      s_RL[yy] = incl;
+      if (lane == (REV ? 0 : 31)) s_rlw[yy / 32] = incl;
+      __syncwarp();
+      if (lane == 0) {
+        // the last row warp to get here publishes u = sum of rowleft, the corner
+        // aggregate; the later of it and the corner warp publishes corner + u
+        __threadfence_block();
+        if (atomicAdd(&s_cnt_row, 1) == TH / 32 - 1) {
+          __threadfence_block();
+          s_cnt_row = 0;
+          A u = AR::zero();
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) top[c] = AR::add(base, cp[c]);
+          for (int g = 0; g < TH / 32; ++g) u = AR::add(u, vload(&s_rlw[g]));
+          vstore(&s_u, u);
+          unsigned long long* cw = P.corner_words + (unsigned long long)t * K;
+          if (pub_col && !stall) publish<A>(cw, u, tagA);
+          __threadfence_block();
+          if (atomicAdd(&s_cnt_corner, 1) == 1) {
+            __threadfence_block();
+            s_cnt_corner = 0;
+            if (pub_col && !stall) publish<A>(cw, AR::add(vload(&s_corner), u), tagI);
+          }
+        }
+      }
+    } else if (warp == CW) {
+      if (lane == 0) {
+        const A c = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+        vstore(&s_corner, c);
+        __threadfence_block();
+        if (atomicAdd(&s_cnt_corner, 1) == 1) {
+          __threadfence_block();
+          s_cnt_corner = 0;
+          if (pub_col && !stall)
+            publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(c, vload(&s_u)),
+                       tagI);
+        }
+      }
+    } else if (tid == PT && producing) {
+      // tile k+S-1 into the stage whose store (tile k-1) has finished reading it
+      const int ps = (st + S - 1) % S;
+      bulk_wait_read_all();
+      producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile, s_img,
+                                                          s_tx, s_ty, s_full);
+      if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
     }
-    const bool tma_out = flags & kOutTma;
+    __syncthreads();
+
+    // ---- D(k): scan with the carries injected, results out ---------------------
     {
-      const int64_t out_pitch = Dp.out_pitch;
-      const int64_t height = Dp.height;
-      const bool vout = (flags & kOutVec) && nvalid == CPT;
-      TOut* out = static_cast<TOut*>(Dp.out) + (y0 + warp * RPW) * out_pitch + xt;
-      // the stage, reused for this thread's results (its inputs are in registers)
+      const ImageView D = image_view(P, cur.img);
+      const uint32_t flags = D.flags;
+      const bool tma_out = flags & kOutTma;
+      const long long x0 = (long long)cur.tx * TW, y0 = (long long)cur.ty * TH;
+      const long long xt = x0 + (long long)lane * CPT;
+      const long long rem = D.width - xt;
+      const int nvalid = rem <= 0 ? 0 : (rem >= CPT ? CPT : (int)rem);
+      const A corner = s_corner;
+      A top[CPT];
+      {
+        const bool has_prev = REV ? (warp < NW - 1) : (warp > 0);
+        A rl_prev = AR::zero();
+        if (has_prev) {
+          // RL of the row just outside the warp: its group's scan plus the groups before it
+          const int yp = REV ? (warp + 1) * RPW : warp * RPW - 1;
+          rl_prev = s_RL[yp];
+#pragma unroll
+          for (int g = 0; g < TH / 32; ++g)
+            if (REV ? (g > yp / 32) : (g < yp / 32)) rl_prev = AR::add(s_rlw[g], rl_prev);
+        }
+        A cp[CPT];
+#pragma unroll
+        for (int i = 0; i < CPT; ++i) {
+          const int c = REV ? CPT - 1 - i : i;
+          cp[c] = AR::add(s_colabove[c * 32 + lane], s_colp[k & 1][warp][c * 32 + lane]);
+          if (i) cp[c] = AR::add(cp[REV ? c + 1 : c - 1], cp[c]);
+        }
+        A incl = cp[REV ? 0 : CPT - 1];
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const A o = REV ? AR::shfl_down(incl, d) : AR::shfl_up(incl, d);
+          if (REV ? (lane + d < 32) : (lane >= d)) incl = AR::add(o, incl);
+        }
+        A ex = REV ? AR::shfl_down(incl, 1) : AR::shfl_up(incl, 1);
+        if (lane == (REV ? 31 : 0)) ex = AR::zero();
+        const A base = AR::add(AR::add(corner, rl_prev), ex);
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) top[c] = AR::add(base, cp[c]);
+      }
+      TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
       TOut* so = reinterpret_cast<TOut*>(stages + st * STAGE_ELEMS) + (warp * RPW) * TW + lane * CPT;
+      RowSeg<TIn, CPT> raw[WIDEN ? RPW : 1];
+      if (WIDEN) {
+        // wider outputs overwrite other threads' inputs: read all inputs first
+#pragma unroll
+        for (int r = 0; r < (WIDEN ? RPW : 1); ++r)
+          raw[r].u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+        __syncthreads();
+      }
+      const int64_t out_pitch = D.out_pitch;
+      const int64_t height = D.height;
+      const bool vout = (flags & kOutVec) && nvalid == CPT;
+      TOut* out = static_cast<TOut*>(D.out) + (y0 + warp * RPW) * out_pitch + xt;
 #pragma unroll
       for (int i = 0; i < RPW; ++i) {
         const int r = REV ? RPW - 1 - i : i;
-        const TIn* x = raw[r].u.e;
-        A run = AR::add(E[r], s_rowleft[warp * RPW + r]);
+        RowSeg<TIn, CPT> x;
+        if (WIDEN) x = raw[WIDEN ? r : 0];
+        else x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+        A run = AR::add(E_cur[r], s_rowleft[warp * RPW + r]);
         TOut o[CPT];
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
-          run = AR::add(run, Cvt<A, TIn>::in(x[c]));
+          run = AR::add(run, Cvt<A, TIn>::in(x.u.e[c]));
           top[c] = AR::add(top[c], run);
           o[c] = OutCvt<TOut, A>::out(top[c]);
         }
@@ -813,18 +896,17 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
           store_seg<TOut, CPT>(out + r * out_pitch, vout, nvalid, o);
         }
       }
-    }
-    // end of the tile: shared vectors may be reused, and with TMA output one
-    // bulk tensor store moves the tile out (clipped at the image edges) and
-    // drains while the CTA goes on with the next tile
-    if (tma_out) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tma_out) {
-      if (tid == PT) {
-        const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[img].tmap_out;
-        tma_store_2d(map, tx * TW, ty * TH, smem_u32(stages + st * STAGE_ELEMS));
+      // end of the tile: shared vectors may be reused; with TMA output one bulk
+      // tensor store moves the tile out (clipped at the image edges) and drains
+      // while the CTA goes on with the next tiles
+      if (tma_out) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tma_out && tid == PT) {
+        const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[cur.img].tmap_out;
+        tma_store_2d(map, cur.tx * TW, cur.ty * TH, smem_u32(stages + st * STAGE_ELEMS));
       }
     }
+    have = have_next;
   }
   if (tid == PT) bulk_wait_all(); // stores read shared memory until they complete
 

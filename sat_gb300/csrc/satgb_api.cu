@@ -26,10 +26,10 @@
 namespace satgb {
 
 const TileConfig kConfigs[kNumConfigs] = {
-    {8, 8, "64-row tiles, 8 warps"},
-    {16, 8, "128-row tiles, 8 warps"},
-    {4, 8, "32-row tiles, 8 warps"},
+    {4, 16, "64-row tiles, 16 warps"},
     {8, 16, "128-row tiles, 16 warps"},
+    {4, 8, "32-row tiles, 8 warps, 2 CTAs per SM"},
+    {2, 16, "32-row tiles, 16 warps"},
 };
 
 namespace {
@@ -376,15 +376,13 @@ int sms_of(int dev) {
   return d.sms;
 }
 
-// Heuristic default when no tuning entry exists: the largest tile whose
-// tile count still gives every SM a few tiles.
+// Heuristic default when no tuning entry exists: 64-row tiles unless the
+// image is too small to give every SM a few of them.
 int default_config(long long width, long long height, int sms, int out_sz) {
   const int cpt = 16 / out_sz;
   const long long tw = 32LL * cpt;
   const long long ntx = (width + tw - 1) / tw;
-  const long long tiles128 = ntx * ((height + 127) / 128);
   const long long tiles64 = ntx * ((height + 63) / 64);
-  if (tiles128 >= 8LL * std::max(1, sms)) return 1;
   if (tiles64 >= 2LL * std::max(1, sms)) return 0;
   return 2;
 }
