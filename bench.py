@@ -223,6 +223,15 @@ def run_gpu(args):
                        "ms_median": round(statistics.median(per_d), 4)}
     sat_gb300.stream_check()
     del xb, yb, xd, yd
+    if not args.no_extra:
+        sub["batch512_u8_u32"] = batch_result(dev, stream, peak)
+        torch.cuda.empty_cache()
+        sub["batch512_u8_u32_packed"] = batch_result(dev, stream, peak, pitched=False)
+        torch.cuda.empty_cache()
+        sub["box_filter_64x3x1024"] = box_result(dev, stream)
+        torch.cuda.empty_cache()
+        sub.update(stress_result(dev, stream, peak))
+        torch.cuda.empty_cache()
 
     # ---- e2e: the same headline SAT through the C ABI with host buffers ---------
     hx = torch.empty((H_HEAD, W_HEAD), dtype=torch.float32, pin_memory=True)
@@ -373,9 +382,179 @@ def run_case(args):
                       "launches": args.steps + args.warmup}))
 
 
+def _log_uniform_sizes(n, lo, hi, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    e = rng.uniform(np.log(lo), np.log(hi), size=(n, 2))
+    return [(int(round(np.exp(a))), int(round(np.exp(b)))) for a, b in e]  # (width, height)
+
+
+def _pitched(h, w, dtype, dev, row_align=128):
+    """An (h, w) view whose rows start every `row_align` bytes, as a pitched
+    allocation (the reference's GpuData, cudaMalloc3D) lays them out."""
+    import torch
+    esz = torch.empty((), dtype=dtype).element_size()
+    pitch = -(-w * esz // row_align) * row_align // esz
+    base_dt = torch.int32 if dtype == torch.uint32 else dtype
+    base = torch.empty((h, pitch), dtype=base_dt, device=dev)
+    if dtype == torch.uint32:
+        base = base.view(torch.uint32)
+    return base[:, :w]
+
+
+def build_batch(dev, seed=512, pitched=True):
+    """512 u8 images, width and height independently log-uniform in
+    [64, 4096], u8 -> u32 outputs; rows pitched to 128 bytes, or packed."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    sizes = _log_uniform_sizes(512, 64, 4096, seed)
+    xs, ys = [], []
+    for w, h in sizes:
+        v = torch.randint(0, 256, (h, w), dtype=torch.uint8, device=dev, generator=g)
+        if pitched:
+            x = _pitched(h, w, torch.uint8, dev)
+            x.copy_(v)
+            xs.append(x)
+            ys.append(_pitched(h, w, torch.uint32, dev))
+        else:
+            xs.append(v)
+            ys.append(torch.empty((h, w), dtype=torch.int32, device=dev).view(torch.uint32))
+    nbytes = sum(w * h * 5 for w, h in sizes)
+    return xs, ys, nbytes
+
+
+def batch_result(dev, stream, peak, pitched=True):
+    """The batch workload as one graph replay of a persistent launch, against
+    the same images as 512 per-image calls."""
+    import torch
+
+    import sat_gb300
+    xs, ys, nbytes = build_batch(dev, pitched=pitched)
+    plan = sat_gb300.BatchPlan(xs, ys, stream=stream)
+    _, per_g = _time_steps(lambda: plan.exec(stream), 20, 3, stream, 0.2)
+    plan.check(stream)
+
+    def per_image():
+        for a, b in zip(xs, ys):
+            sat_gb300.sat(a, torch.uint32, out=b)
+
+    _, per_i = _time_steps(per_image, 5, 2, stream, 0.0)
+    sat_gb300.stream_check()
+    gm, im = statistics.median(per_g), statistics.median(per_i)
+    res = {"images": len(xs), "bytes": int(nbytes), "graph_ms": round(gm, 4),
+           "graph_gbs": round(nbytes / (gm / 1e3) / GB, 1), "frac_of_peak": round(nbytes / (gm / 1e3) / GB / peak, 4),
+           "per_image_ms": round(im, 4), "per_image_gbs": round(nbytes / (im / 1e3) / GB, 1),
+           "tiles": plan.info()["n_tiles"], "rows": "pitched to 128 B" if pitched else "packed"}
+    plan.close()
+    return res
+
+
+def build_box(dev, n=64, c=3, h=1024, w=1024, radii=(3, 7, 15), seed=99):
+    """The box-filter layer workload: f32 N(0,1) of shape (n, c, h, w), box
+    means for three radii, gradient W ~ N(0,1) of the means' shape."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    x = torch.randn((n, c, h, w), dtype=torch.float32, device=dev, generator=g)
+    wts = torch.randn((n, c, len(radii), h, w), dtype=torch.float32, device=dev, generator=g)
+    return x, wts, radii
+
+
+def box_result(dev, stream):
+    """Forward (SAT + box means) against forward + backward (dL/dmeans = W,
+    adjoint gather + reverse SAT) of the box-filter layer."""
+    import torch
+
+    import sat_gb300
+    x, wts, radii = build_box(dev)
+    xg = x.clone().requires_grad_(True)
+
+    def fwd():
+        with torch.no_grad():
+            sat_gb300.box_filter_means(x, radii)
+
+    def fwd_bwd():
+        xg.grad = None
+        m = sat_gb300.box_filter_means(xg, radii)
+        m.backward(wts)
+
+    _, per_f = _time_steps(fwd, 10, 3, stream, 0.2)
+    _, per_fb = _time_steps(fwd_bwd, 10, 3, stream, 0.2)
+    sat_gb300.stream_check()
+    f, fb = statistics.median(per_f), statistics.median(per_fb)
+    sat_bytes = x.numel() * 8
+    return {"shape": list(x.shape), "radii": list(radii), "fwd_ms": round(f, 4), "fwd_bwd_ms": round(fb, 4),
+            "fwd_bwd_over_fwd": round(fb / f, 3), "forward_sat_bytes": int(sat_bytes)}
+
+
+def stress_result(dev, stream, peak):
+    """32768^2 u8 -> u32 (wrapping mod 2^32) and 16384^2 f32 compensated."""
+    import torch
+
+    import sat_gb300
+    res = {}
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    xb = torch.randint(0, 256, (32768, 32768), dtype=torch.uint8, device=dev, generator=g)
+    yb = torch.empty((32768, 32768), dtype=torch.int32, device=dev).view(torch.uint32)
+    _, per = _time_steps(lambda: sat_gb300.sat(xb, torch.uint32, out=yb), 5, 3, stream, 0.0)
+    nb = xb.numel() * 5
+    res["u8_u32_32768"] = {"ms_median": round(statistics.median(per), 4),
+                           "gbs": round(nb / (statistics.median(per) / 1e3) / GB, 1)}
+    del xb, yb
+    xf = torch.rand((16384, 16384), dtype=torch.float32, device=dev, generator=g)
+    yf = torch.empty_like(xf)
+    _, per = _time_steps(lambda: sat_gb300.sat(xf, torch.float32, mode="compensated", out=yf), 10, 3, stream, 0.0)
+    nb = xf.numel() * 8
+    res["f32_compensated_16384"] = {"ms_median": round(statistics.median(per), 4),
+                                    "gbs": round(nb / (statistics.median(per) / 1e3) / GB, 1)}
+    sat_gb300.stream_check()
+    for v in res.values():
+        v["frac_of_peak"] = round(v["gbs"] / peak, 4)
+    return res
+
+
+def run_workload(args):
+    """Short runs of the non-SAT workloads (for ncu captures and quick timing)."""
+    import torch
+
+    import sat_gb300
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream()
+    if args.case in ("batch512", "batch512_packed"):
+        xs, ys, nbytes = build_batch(dev, pitched=args.case == "batch512")
+        plan = sat_gb300.BatchPlan(xs, ys, stream=stream)
+        _, per = _time_steps(lambda: plan.exec(stream), args.steps, args.warmup, stream, 0.0)
+        plan.check(stream)
+        med = statistics.median(per)
+        print(json.dumps({"case": args.case, "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1)}))
+    elif args.case in ("box_fwd", "box_fwdbwd"):
+        n = 8 if args.small else 64
+        x, wts, radii = build_box(dev, n=n)
+        xg = x.clone().requires_grad_(True)
+
+        def step():
+            if args.case == "box_fwd":
+                with torch.no_grad():
+                    sat_gb300.box_filter_means(x, radii)
+            else:
+                xg.grad = None
+                sat_gb300.box_filter_means(xg, radii).backward(wts)
+
+        _, per = _time_steps(step, args.steps, args.warmup, stream, 0.0)
+        sat_gb300.stream_check()
+        print(json.dumps({"case": args.case, "n": n, "ms_median": round(statistics.median(per), 5)}))
+
+
+WORKLOADS = ("batch512", "batch512_packed", "box_fwd", "box_fwdbwd")
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=sorted(CASES))
+    ap.add_argument("--case", default=None, choices=sorted(CASES) + list(WORKLOADS))
+    ap.add_argument("--small", action="store_true", help="box workloads: 8 images instead of 64")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batch, box-filter and stress sub-results")
     ap.add_argument("--config", type=int, default=-1, help="force a tile configuration (--case only)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
@@ -388,7 +567,7 @@ def main():
     if args.case:
         from sat_gb300 import build as B
         B.build()
-        run_case(args)
+        run_workload(args) if args.case in WORKLOADS else run_case(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

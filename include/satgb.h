@@ -139,6 +139,39 @@ typedef struct {
 
 satgb_status satgb_sat_ex(const satgb_sat_desc* desc, satgb_stream stream);
 
+/* The same SAT for a stack of n_planes equally sized images (e.g. the N*C
+ * planes of an N x C x H x W tensor), plane p starting at d_in + p *
+ * in_plane_stride and d_out + p * out_plane_stride (elements); each plane gets
+ * its own SAT, all in one launch.  No reference counterpart. */
+satgb_status satgb_sat_planes(const satgb_sat_desc* desc, int64_t n_planes, int64_t in_plane_stride,
+                              int64_t out_plane_stride, satgb_stream stream);
+
+/* ------------------------------------------------------------------------- */
+/* Box filters from a SAT (f32), the main use of a summed-area table.  No     */
+/* reference counterpart.  For radius r the box mean at (y,x) is the mean of  */
+/* the input over rows [y-r, y+r] and columns [x-r, x+r] clipped to the       */
+/* image, read from the inclusive SAT S of the input by four corners:         */
+/*   (S(yb,xb) - S(ya-1,xb) - S(yb,xa-1) + S(ya-1,xa-1)) / area.              */
+/* Up to four radii are filtered in one pass over n_planes planes.            */
+/* ------------------------------------------------------------------------- */
+#define SATGB_MAX_RADII 4
+typedef struct {
+  int64_t width, height, n_planes;
+  void* d_sat;            /* forward: the SAT (read); backward: dL/dSAT (written) */
+  int64_t sat_pitch, sat_plane_stride;
+  int n_radii;            /* 1 .. SATGB_MAX_RADII */
+  int radius[SATGB_MAX_RADII];
+  void* d_box[SATGB_MAX_RADII]; /* forward: box means (written); backward: dL/dmeans (read) */
+  int64_t box_pitch, box_plane_stride;
+} satgb_box_desc;
+
+/* Box means of every radius from the SAT. */
+satgb_status satgb_box_filter_fwd(const satgb_box_desc* desc, satgb_stream stream);
+/* The adjoint of satgb_box_filter_fwd: dL/dSAT from the gradients of all the
+ * radii's means (the four-corner scatter, computed as a gather so it is
+ * deterministic).  d_sat is overwritten. */
+satgb_status satgb_box_filter_bwd(const satgb_box_desc* desc, satgb_stream stream);
+
 /* The same single-image SAT as satgb_sat_ex, for callers that cannot allocate
  * device memory: code running inside an allocator or memory-pool callback, in
  * a process whose device memory a framework has reserved up front, or in a

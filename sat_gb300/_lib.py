@@ -57,6 +57,17 @@ class satgb_image(ctypes.Structure):
                 ("out_pitch", ctypes.c_int64), ("width", ctypes.c_int64), ("height", ctypes.c_int64)]
 
 
+MAX_RADII = 4
+
+
+class satgb_box_desc(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int64), ("height", ctypes.c_int64), ("n_planes", ctypes.c_int64),
+                ("d_sat", ctypes.c_void_p), ("sat_pitch", ctypes.c_int64), ("sat_plane_stride", ctypes.c_int64),
+                ("n_radii", ctypes.c_int), ("radius", ctypes.c_int * MAX_RADII),
+                ("d_box", ctypes.c_void_p * MAX_RADII), ("box_pitch", ctypes.c_int64),
+                ("box_plane_stride", ctypes.c_int64)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _I64 = ctypes.c_int64
@@ -90,8 +101,9 @@ SIGNATURES = {
     "satgb_launch_count": (_I64, []),
     "satgb_debug_stall_tile": (_ST, [_I64]),
     "satgb_version": (_I, []),
-    "satgb_box_filter_fwd": (_ST, [_I, _P, _I64, _P, _I64, _I64, _I64, _I64, _I64, _P, _P]),
-    "satgb_box_filter_bwd": (_ST, [_I, _P, _I64, _P, _I64, _I64, _I64, _I64, _I64, _P, _P]),
+    "satgb_sat_planes": (_ST, [ctypes.POINTER(satgb_sat_desc), _I64, _I64, _I64, _P]),
+    "satgb_box_filter_fwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),
+    "satgb_box_filter_bwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),
 }
 
 _lib = None

@@ -126,18 +126,96 @@ ALGORITHMS = {
 }
 
 
+def _planes_args(t: torch.Tensor):
+    """(ptr, pitch, width, height, n_planes, plane_stride) of a (..., H, W)
+    tensor whose leading dimensions collapse into one plane stride."""
+    if t.dim() < 3:
+        raise SatError(_lib.ERR_INVALID_ARG, f"expected a (..., H, W) tensor, got shape {tuple(t.shape)}")
+    h, w = t.shape[-2], t.shape[-1]
+    try:
+        v = t.view(-1, h, w)
+    except RuntimeError:
+        raise SatError(_lib.ERR_INVALID_ARG, "leading dimensions must collapse into one plane stride") from None
+    if w > 1 and v.stride(2) != 1:
+        raise SatError(_lib.ERR_INVALID_ARG, "image rows must be contiguous (stride(-1) == 1)")
+    pitch = v.stride(1) if h > 1 else max(w, v.stride(1))
+    n = v.shape[0]
+    plane = v.stride(0) if n > 1 else pitch * h
+    return v.data_ptr(), int(pitch), int(w), int(h), int(n), int(plane)
+
+
 def sat(src: torch.Tensor, out_dtype=None, mode: str = "plain", reverse: bool = False, out=None,
         stream=None) -> torch.Tensor:
-    """SAT (or, with reverse=True, the suffix SAT) of a 2-D image; mode
-    "compensated" carries two-sum error terms (f32 outputs)."""
+    """SAT (or, with reverse=True, the suffix SAT) of a 2-D image, or of every
+    (H, W) plane of a (..., H, W) tensor in one launch; mode "compensated"
+    carries two-sum error terms (f32 outputs)."""
     _check_cuda(src)
     out = _prep_out(src, out_dtype, out)
     _check_cuda(out)
+    direction = REVERSE if reverse else FORWARD
+    if src.dim() >= 3:
+        ip, ipitch, w, h, n, iplane = _planes_args(src)
+        op, opitch, _, _, _, oplane = _planes_args(out)
+        d = _lib.satgb_sat_desc(dtype_code(src.dtype), dtype_code(out.dtype), _MODES[mode], direction,
+                                ip, ipitch, op, opitch, w, h)
+        check(_lib.load().satgb_sat_planes(ctypes.byref(d), n, iplane, oplane, _stream_handle(stream)))
+        return out
     ip, ipitch, w, h = _image_args(src)
     op, opitch, _, _ = _image_args(out)
-    d = _lib.satgb_sat_desc(dtype_code(src.dtype), dtype_code(out.dtype), _MODES[mode],
-                            REVERSE if reverse else FORWARD, ip, ipitch, op, opitch, w, h)
+    d = _lib.satgb_sat_desc(dtype_code(src.dtype), dtype_code(out.dtype), _MODES[mode], direction,
+                            ip, ipitch, op, opitch, w, h)
     check(_lib.load().satgb_sat_ex(ctypes.byref(d), _stream_handle(stream)))
+    return out
+
+
+def _box_desc(sat_t: torch.Tensor, boxes: torch.Tensor, radii: Sequence[int]):
+    """satgb_box_desc for a (..., H, W) f32 SAT and a (..., R, H, W) f32 box
+    tensor (one (H, W) plane per radius)."""
+    if sat_t.dtype != torch.float32 or boxes.dtype != torch.float32:
+        raise SatError(_lib.ERR_UNSUPPORTED_TYPES, "box filters take f32 tensors")
+    radii = [int(r) for r in radii]
+    if not 1 <= len(radii) <= _lib.MAX_RADII or min(radii) < 0:
+        raise SatError(_lib.ERR_INVALID_ARG, f"1..{_lib.MAX_RADII} non-negative radii, got {radii}")
+    if boxes.shape != sat_t.shape[:-2] + (len(radii),) + sat_t.shape[-2:]:
+        raise SatError(_lib.ERR_INVALID_ARG, "box tensor must be (..., R, H, W)")
+    _check_cuda(sat_t, boxes)
+    s3 = sat_t if sat_t.dim() >= 3 else sat_t.unsqueeze(0)
+    sp, spitch, w, h, n, splane = _planes_args(s3)
+    b4 = boxes.reshape((-1, len(radii)) + boxes.shape[-2:]) if boxes.dim() >= 4 else boxes.unsqueeze(0)
+    if b4.data_ptr() != boxes.data_ptr() or b4.stride(-1) != 1:
+        raise SatError(_lib.ERR_INVALID_ARG, "box tensor must be contiguous in its last dimension")
+    d = _lib.satgb_box_desc()
+    d.width, d.height, d.n_planes = w, h, n
+    d.d_sat, d.sat_pitch, d.sat_plane_stride = sp, spitch, splane
+    d.n_radii = len(radii)
+    esz = boxes.element_size()
+    for i, r in enumerate(radii):
+        d.radius[i] = r
+        d.d_box[i] = b4.data_ptr() + i * b4.stride(1) * esz
+    d.box_pitch = b4.stride(2) if h > 1 else max(w, b4.stride(2))
+    d.box_plane_stride = b4.stride(0) if n > 1 else d.box_pitch * h
+    return d
+
+
+def box_means_from_sat(sat_t: torch.Tensor, radii: Sequence[int], out=None, stream=None) -> torch.Tensor:
+    """Clipped box means of every radius from an f32 SAT: (..., H, W) ->
+    (..., R, H, W)."""
+    if out is None:
+        out = torch.empty(sat_t.shape[:-2] + (len(radii),) + sat_t.shape[-2:], dtype=torch.float32,
+                          device=sat_t.device)
+    d = _box_desc(sat_t, out, radii)
+    check(_lib.load().satgb_box_filter_fwd(ctypes.byref(d), _stream_handle(stream)))
+    return out
+
+
+def box_means_adjoint(grad_boxes: torch.Tensor, radii: Sequence[int], out=None, stream=None) -> torch.Tensor:
+    """The adjoint of box_means_from_sat: dL/dSAT (..., H, W) from dL/dmeans
+    (..., R, H, W)."""
+    if out is None:
+        out = torch.empty(grad_boxes.shape[:-3] + grad_boxes.shape[-2:], dtype=torch.float32,
+                          device=grad_boxes.device)
+    d = _box_desc(out, grad_boxes, radii)
+    check(_lib.load().satgb_box_filter_bwd(ctypes.byref(d), _stream_handle(stream)))
     return out
 
 

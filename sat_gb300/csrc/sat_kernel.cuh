@@ -59,16 +59,27 @@
 
 namespace satgb {
 
+// One image, or a stack of `planes` equally sized images at a fixed stride
+// (the planes of an N x C x H x W tensor), each with its own SAT.
 struct ImageDesc {
-  CUtensorMap tmap_in;  // 2-D tiled map of the input (valid when flags & kInTma)
-  CUtensorMap tmap_out; // 2-D tiled map of the output (valid when flags & kOutTma)
+  CUtensorMap tmap_in;  // 3-D tiled map (x, y, plane) of the input (valid when flags & kInTma)
+  CUtensorMap tmap_out; // 3-D tiled map of the output (valid when flags & kOutTma)
   const void* in;
   void* out;
   int64_t in_pitch;  // elements
   int64_t out_pitch; // elements
   int64_t width, height;
+  int64_t planes;          // >= 1
+  int64_t in_plane;        // plane stride of the input, elements
+  int64_t out_plane;       // plane stride of the output, elements
+  int64_t tiles_per_plane; // ntx * nty
   int64_t tile_base; // global index of the image's first tile
-  int32_t ntx, nty;  // tiles across / down
+  // Columns the tensor maps cover: the width rounded down to whole 16-byte
+  // chunks.  TMA moves whole chunks, so a map that reached into a row's last,
+  // partial chunk could write the caller's row padding; the columns past the
+  // map ([tma_*_w, width)) are loaded and stored with plain accesses.
+  int64_t tma_in_w, tma_out_w;
+  int32_t ntx, nty;  // tiles across / down (per plane)
   uint32_t flags;    // kInVec | kOutVec | kInTma | kOutTma
   uint32_t pad;
 };
@@ -198,16 +209,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
       : "memory");
 }
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int y, int z, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
                    reinterpret_cast<uint64_t>(map)),
-               "r"(x), "r"(y), "r"(src)
+               "r"(x), "r"(y), "r"(z), "r"(src)
                : "memory");
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
@@ -401,7 +412,7 @@ __device__ __forceinline__ A resolve(EarlyWin<A>& e, const unsigned long long* b
 struct ImageView {
   const void* in;
   void* out;
-  int64_t in_pitch, out_pitch, width, height;
+  int64_t in_pitch, out_pitch, width, height, in_plane, out_plane, tma_in_w, tma_out_w;
   int32_t ntx, nty;
   uint32_t flags;
 };
@@ -415,6 +426,10 @@ __device__ __forceinline__ ImageView image_view(const SatParams& P, int img) {
     v.out_pitch = P.img0.out_pitch;
     v.width = P.img0.width;
     v.height = P.img0.height;
+    v.in_plane = P.img0.in_plane;
+    v.out_plane = P.img0.out_plane;
+    v.tma_in_w = P.img0.tma_in_w;
+    v.tma_out_w = P.img0.tma_out_w;
     v.ntx = P.img0.ntx;
     v.nty = P.img0.nty;
     v.flags = P.img0.flags;
@@ -426,6 +441,10 @@ __device__ __forceinline__ ImageView image_view(const SatParams& P, int img) {
     v.out_pitch = D->out_pitch;
     v.width = D->width;
     v.height = D->height;
+    v.in_plane = D->in_plane;
+    v.out_plane = D->out_plane;
+    v.tma_in_w = D->tma_in_w;
+    v.tma_out_w = D->tma_out_w;
     v.ntx = D->ntx;
     v.nty = D->nty;
     v.flags = D->flags;
@@ -452,7 +471,7 @@ struct TileShape {
 // Returns false once the tickets are exhausted (the stage then carries -1).
 template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES>
 __device__ __forceinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
-                                        long long* s_tile, int* s_img, int* s_tx, int* s_ty,
+                                        long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
                                         unsigned long long* s_full) {
   const uint32_t bar = smem_u32(&s_full[st]);
   if ((long long)tk >= P.n_tiles) {
@@ -473,15 +492,19 @@ __device__ __forceinline__ bool produce(const SatParams& P, unsigned long long t
   }
   const ImageDesc* D = (P.n_images == 1) ? &P.img0 : &P.images[img];
   const int ntx = D->ntx, nty = D->nty;
+  // planes one after the other; anti-diagonal order inside a plane
+  const long long local = q - D->tile_base;
+  const long long pl = local / D->tiles_per_plane;
   int tx, ty;
-  diag_tile(q - D->tile_base, ntx, nty, tx, ty);
-  s_tile[st] = D->tile_base + (long long)ty * ntx + tx;
+  diag_tile(local - pl * D->tiles_per_plane, ntx, nty, tx, ty);
+  s_tile[st] = D->tile_base + pl * D->tiles_per_plane + (long long)ty * ntx + tx;
   s_img[st] = img;
   s_tx[st] = tx;
   s_ty[st] = ty;
+  s_pl[st] = (int)pl;
   if (D->flags & kInTma) {
     mbar_arrive_expect_tx(bar, (uint32_t)STAGE_BYTES);
-    tma_load_2d(smem_u32(stage_ptr), &D->tmap_in, tx * TW, ty * TH, bar);
+    tma_load_3d(smem_u32(stage_ptr), &D->tmap_in, tx * TW, ty * TH, (int)pl, bar);
   } else {
     mbar_arrive(bar);
   }
@@ -552,7 +575,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   __shared__ int s_cnt_row, s_cnt_corner; // arrivals of the row warps / of {rows, corner}
   __shared__ long long s_tile[S];   // spatial tile index per stage (-1: no more tiles)
   __shared__ int s_img[S];
-  __shared__ int s_tx[S], s_ty[S];
+  __shared__ int s_tx[S], s_ty[S], s_pl[S];
   __shared__ __align__(8) unsigned long long s_full[S];
 
   const int tid = threadIdx.x;
@@ -577,7 +600,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       if (producing)
         producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, atomicAdd(&P.ws->ticket, 1ull), s,
                                                             stages + s * STAGE_ELEMS, s_tile, s_img, s_tx, s_ty,
-                                                            s_full);
+                                                            s_pl, s_full);
     }
     if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
   }
@@ -586,7 +609,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   // ---- per-tile state carried from the local phase to the output phase ---------
   struct Tile {
     long long t;
-    int tx, ty, img;
+    int tx, ty, img, p;
   };
   Tile nxt, cur;
   A E_nxt[RPW], E_cur[RPW];
@@ -605,6 +628,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     nxt.tx = s_tx[st];
     nxt.ty = s_ty[st];
     nxt.img = s_img[st];
+    nxt.p = s_pl[st];
     const ImageView D = image_view(P, nxt.img);
     const uint32_t flags = D.flags;
     const long long x0 = (long long)nxt.tx * TW, y0 = (long long)nxt.ty * TH;
@@ -616,13 +640,21 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
     for (int c = 0; c < CPT; ++c) colp[c] = AR::zero();
     const bool tma = flags & kInTma;
-    const TIn* gin = static_cast<const TIn*>(D.in) + (y0 + warp * RPW) * D.in_pitch + xt;
+    const TIn* gin = static_cast<const TIn*>(D.in) + (long long)nxt.p * D.in_plane + (y0 + warp * RPW) * D.in_pitch + xt;
     const bool vin = (flags & kInVec) && nvalid == CPT;
+    const bool tail_in = tma && nvalid > 0 && xt + nvalid > D.tma_in_w;
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
       RowSeg<TIn, CPT> x;
       if (tma) {
         x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+        if (tail_in && y0 + warp * RPW + r < D.height) {
+          // columns past the map arrived as zeros: load them and patch the stage
+#pragma unroll
+          for (int c = 0; c < CPT; ++c)
+            if (xt + c >= D.tma_in_w && c < nvalid) x.u.e[c] = gin[r * D.in_pitch + c];
+          *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = x.u.v;
+        }
       } else {
         // no TMA for this image: load from global memory and park the values in
         // the stage for the output phase (each thread reads back only its own block)
@@ -809,7 +841,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       const int ps = (st + S - 1) % S;
       bulk_wait_read_all();
       producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile, s_img,
-                                                          s_tx, s_ty, s_full);
+                                                          s_tx, s_ty, s_pl, s_full);
       if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
     }
     __syncthreads();
@@ -868,7 +900,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       const int64_t out_pitch = D.out_pitch;
       const int64_t height = D.height;
       const bool vout = (flags & kOutVec) && nvalid == CPT;
-      TOut* out = static_cast<TOut*>(D.out) + (y0 + warp * RPW) * out_pitch + xt;
+      TOut* out = static_cast<TOut*>(D.out) + (long long)cur.p * D.out_plane + (y0 + warp * RPW) * out_pitch + xt;
+      const bool tail_out = tma_out && nvalid > 0 && xt + nvalid > D.tma_out_w;
 #pragma unroll
       for (int i = 0; i < RPW; ++i) {
         const int r = REV ? RPW - 1 - i : i;
@@ -892,6 +925,12 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
           for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
           *reinterpret_cast<uint4*>(so + r * TW) = u.v;
+          if (tail_out && y0 + warp * RPW + r < height) {
+            // columns past the map: plain stores
+#pragma unroll
+            for (int c = 0; c < CPT; ++c)
+              if (xt + c >= D.tma_out_w && c < nvalid) out[r * out_pitch + c] = o[c];
+          }
         } else if (y0 + warp * RPW + r < height && nvalid > 0) {
           store_seg<TOut, CPT>(out + r * out_pitch, vout, nvalid, o);
         }
@@ -903,7 +942,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       __syncthreads();
       if (tma_out && tid == PT) {
         const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[cur.img].tmap_out;
-        tma_store_2d(map, cur.tx * TW, cur.ty * TH, smem_u32(stages + st * STAGE_ELEMS));
+        tma_store_3d(map, cur.tx * TW, cur.ty * TH, cur.p, smem_u32(stages + st * STAGE_ELEMS));
       }
     }
     have = have_next;

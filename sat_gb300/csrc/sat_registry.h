@@ -45,9 +45,11 @@ const Variant* variants_f64(int* n);
 
 const Variant* find_variant(int in_t, int out_t, int mode, int dir, int cfg);
 
-// Fills `d` for one image (pointers, sizes, tile grid, alignment flags) and,
-// when the input rows are 16-byte aligned, its TMA tensor map.
+// Fills `d` for one image or a stack of `planes` images at the given plane
+// strides (pointers, sizes, tile grid, alignment flags) and, where TMA can
+// address the rows, its tensor maps.
 void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const void* in, void* out,
-                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base);
+                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base,
+                     int64_t planes, int64_t in_plane, int64_t out_plane);
 
 }  // namespace satgb

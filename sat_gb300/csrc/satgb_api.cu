@@ -58,65 +58,84 @@ size_t elem_bytes(int t) {
 }
 }  // namespace
 
+namespace {
+// Rank-3 tiled map (x, y, plane) with a TW x TH x 1 box; false when the
+// driver rejects it (the image then uses plain loads or stores).
+bool encode_map(CUtensorMap* m, int t, const void* base, int64_t width, int64_t height, int64_t pitch,
+                int64_t planes, int64_t plane, int tw, int th) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+  if (!enc) return false;
+  const int64_t sz = (int64_t)elem_bytes(t);
+  CUtensorMapDataType dt = sz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
+                           : t == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
+                           : t == 5 ? CU_TENSOR_MAP_DATA_TYPE_INT32
+                           : t == 6 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                    : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)height, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)(pitch * sz), (cuuint64_t)(plane * sz)};
+  cuuint32_t box[3] = {(cuuint32_t)tw, (cuuint32_t)th, 1u};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, dt, 3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// TMA needs the base, the row pitch and the plane stride in multiples of 16
+// bytes.  It moves whole 16-byte chunks of a row, so the map covers only the
+// row's whole chunks (tma_columns); the kernel moves the rest of each row,
+// fewer than 16 bytes, with plain accesses.  Other images use plain loads and
+// stores throughout.
+bool tma_ok(const void* base, int64_t width, int64_t height, int64_t pitch, int64_t planes, int64_t plane,
+            size_t sz) {
+  return ((uintptr_t)base % 16) == 0 && ((size_t)pitch * sz) % 16 == 0 && ((size_t)plane * sz) % 16 == 0 &&
+         (size_t)width * sz >= 16 && width < (1LL << 32) && height < (1LL << 32) && planes < (1LL << 31);
+}
+
+int64_t tma_columns(int64_t width, size_t sz) { return (int64_t)(((size_t)width * sz / 16) * 16 / sz); }
+}  // namespace
+
 void fill_image_desc(ImageDesc& d, const Variant* v, int in_t, int out_t, const void* in, void* out,
-                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base) {
+                     int64_t in_pitch, int64_t out_pitch, int64_t width, int64_t height, int64_t tile_base,
+                     int64_t planes, int64_t in_plane, int64_t out_plane) {
   std::memset(&d, 0, sizeof d);
   const size_t in_sz = elem_bytes(in_t), out_sz = elem_bytes(out_t);
+  if (planes < 1) planes = 1;
+  if (planes == 1) {
+    // one image: any plane stride past its last element will do
+    in_plane = in_pitch * height;
+    out_plane = out_pitch * height;
+    in_plane += (16 - (in_plane * (int64_t)in_sz) % 16) % 16 / (int64_t)in_sz;
+    out_plane += (16 - (out_plane * (int64_t)out_sz) % 16) % 16 / (int64_t)out_sz;
+  }
   d.in = in;
   d.out = out;
   d.in_pitch = in_pitch;
   d.out_pitch = out_pitch;
   d.width = width;
   d.height = height;
+  d.planes = planes;
+  d.in_plane = in_plane;
+  d.out_plane = out_plane;
   d.tile_base = tile_base;
   d.ntx = (int32_t)((width + v->TW - 1) / v->TW);
   d.nty = (int32_t)((height + v->TH - 1) / v->TH);
+  d.tiles_per_plane = (int64_t)d.ntx * d.nty;
   const int cpt = v->TW / 32;
   const size_t seg_in = (size_t)cpt * in_sz;
   uint32_t flags = 0;
-  if (((uintptr_t)in % seg_in) == 0 && ((size_t)in_pitch * in_sz) % seg_in == 0) flags |= kInVec;
-  if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0) flags |= kOutVec;
-  // TMA moves whole 16-byte chunks of a row, so it is used only when the
-  // base, the row pitch and the row's length are all multiples of 16 bytes:
-  // then no chunk reaches into a row's padding or past the buffer.
-  // Other images use plain loads and stores.
-  if (((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * in_sz) % 16 == 0 && ((size_t)width * in_sz) % 16 == 0 &&
-      width < (1LL << 32) && height < (1LL << 32)) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
-    if (enc) {
-      CUtensorMapDataType dt = in_sz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8
-                               : in_t == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
-                               : in_t == 5 ? CU_TENSOR_MAP_DATA_TYPE_INT32
-                               : in_t == 6 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                           : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-      cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
-      cuuint64_t strides[1] = {(cuuint64_t)(in_pitch * (int64_t)in_sz)};
-      cuuint32_t box[2] = {(cuuint32_t)v->TW, (cuuint32_t)v->TH};
-      cuuint32_t estr[2] = {1, 1};
-      CUresult r = enc(&d.tmap_in, dt, 2, const_cast<void*>(in), dims, strides, box, estr,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r == CUDA_SUCCESS) flags |= kInTma;
-    }
-  }
-  if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0 && ((size_t)width * out_sz) % 16 == 0 &&
-      width < (1LL << 32) && height < (1LL << 32)) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
-    if (enc) {
-      CUtensorMapDataType dt = out_t == 4 ? CU_TENSOR_MAP_DATA_TYPE_UINT32
-                               : out_t == 5 ? CU_TENSOR_MAP_DATA_TYPE_INT32
-                               : out_t == 6 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                            : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-      cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
-      cuuint64_t strides[1] = {(cuuint64_t)(out_pitch * (int64_t)out_sz)};
-      cuuint32_t box[2] = {(cuuint32_t)v->TW, (cuuint32_t)v->TH};
-      cuuint32_t estr[2] = {1, 1};
-      CUresult r = enc(&d.tmap_out, dt, 2, out, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r == CUDA_SUCCESS) flags |= kOutTma;
-    }
-  }
+  if (((uintptr_t)in % seg_in) == 0 && ((size_t)in_pitch * in_sz) % seg_in == 0 &&
+      ((size_t)in_plane * in_sz) % seg_in == 0)
+    flags |= kInVec;
+  if (((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * out_sz) % 16 == 0 && ((size_t)out_plane * out_sz) % 16 == 0)
+    flags |= kOutVec;
+  d.tma_in_w = tma_columns(width, in_sz);
+  d.tma_out_w = tma_columns(width, out_sz);
+  if (tma_ok(in, width, height, in_pitch, planes, in_plane, in_sz) &&
+      encode_map(&d.tmap_in, in_t, in, d.tma_in_w, height, in_pitch, planes, in_plane, v->TW, v->TH))
+    flags |= kInTma;
+  if (tma_ok(out, width, height, out_pitch, planes, out_plane, out_sz) &&
+      encode_map(&d.tmap_out, out_t, out, d.tma_out_w, height, out_pitch, planes, out_plane, v->TW, v->TH))
+    flags |= kOutTma;
   d.flags = flags;
 }
 
@@ -376,13 +395,15 @@ int sms_of(int dev) {
   return d.sms;
 }
 
-// Heuristic default when no tuning entry exists: 64-row tiles unless the
-// image is too small to give every SM a few of them.
+// Heuristic default when no tuning entry exists: the largest tiles that
+// still give every SM several of them.
 int default_config(long long width, long long height, int sms, int out_sz) {
   const int cpt = 16 / out_sz;
   const long long tw = 32LL * cpt;
   const long long ntx = (width + tw - 1) / tw;
+  const long long tiles128 = ntx * ((height + 127) / 128);
   const long long tiles64 = ntx * ((height + 63) / 64);
+  if (tiles128 >= 8LL * std::max(1, sms)) return 1;
   if (tiles64 >= 2LL * std::max(1, sms)) return 0;
   return 2;
 }
@@ -426,7 +447,8 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
 
 satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in, long long in_pitch,
                         void* d_out, long long out_pitch, long long width, long long height,
-                        cudaStream_t s, int force_cfg) {
+                        cudaStream_t s, int force_cfg, long long planes = 1, long long in_plane = 0,
+                        long long out_plane = 0) {
   const size_t in_sz = dtype_size(in_t), out_sz = dtype_size(out_t);
   if (!in_sz || !out_sz) return fail(SATGB_ERR_INVALID_ARG, "unknown dtype code (%d, %d)", in_t, out_t);
   if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED) return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
@@ -434,22 +456,39 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   if (!pair_offered(in_t, out_t, mode))
     return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair %s -> %s%s not offered", dtype_name(in_t), dtype_name(out_t),
                 mode == SATGB_MODE_COMPENSATED ? " (compensated)" : "");
+  if (planes < 0) return fail(SATGB_ERR_INVALID_ARG, "negative plane count");
+  if (planes == 0) return SATGB_OK;
   ImgCheck c{d_in, d_out, in_pitch, out_pitch, width, height};
   satgb_status st = validate_image(c, in_sz, out_sz);
   if (st != SATGB_OK) return st;
   if (width == 0 || height == 0) return SATGB_OK;
+  if (planes > 1) {
+    // planes may not overlap each other; the whole stacks are the same buffer or disjoint
+    const long long in_span = (height - 1) * in_pitch + width, out_span = (height - 1) * out_pitch + width;
+    if (in_plane < in_span || out_plane < out_span)
+      return fail(SATGB_ERR_INVALID_ARG, "plane stride smaller than a plane (%lld in, %lld out)", in_plane, out_plane);
+    const long long lim = INT64_MAX / 16;
+    if (planes > lim / in_plane || planes > lim / out_plane) return fail(SATGB_ERR_OVERFLOW, "plane stack overflows");
+    const char* ib = (const char*)d_in;
+    const char* ie = ib + ((planes - 1) * in_plane + in_span) * (long long)in_sz;
+    const char* ob = (const char*)d_out;
+    const char* oe = ob + ((planes - 1) * out_plane + out_span) * (long long)out_sz;
+    const bool same = ib == ob && in_sz == out_sz && in_pitch == out_pitch && in_plane == out_plane;
+    if (!same && ib < oe && ob < ie) return fail(SATGB_ERR_INVALID_ARG, "input and output stacks overlap");
+  }
 
   std::lock_guard<std::mutex> lk(g_mu);
   int dev = 0;
   st = get_device(&dev);
   if (st != SATGB_OK) return st;
-  int cfg = force_cfg >= 0 ? force_cfg : choose_config_locked(in_t, out_t, mode, dir, width, height, dev);
+  int cfg = force_cfg >= 0 ? force_cfg
+                           : choose_config_locked(in_t, out_t, mode, dir, width, height * std::max(1LL, planes), dev);
   const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
   ImageDesc d;
-  fill_image_desc(d, v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, 0);
-  const long long n_tiles = (long long)d.ntx * d.nty;
+  fill_image_desc(d, v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, 0, planes, in_plane, out_plane);
+  const long long n_tiles = (long long)d.ntx * d.nty * d.planes;
   if ((long long)d.ntx * v->TW < width || n_tiles > (1LL << 40))
     return fail(SATGB_ERR_OVERFLOW, "image too large (%lld x %lld)", width, height);
   Workspace& ws = g_ws[std::make_pair(dev, (void*)s)];
@@ -471,6 +510,13 @@ struct satgb_batch_plan_s {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
 };
+
+namespace satgb {
+// Shared with the other translation units of the library (box filters).
+satgb_status api_fail(satgb_status st, const char* msg) { return fail(st, "%s", msg); }
+satgb_status api_cuda_fail(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+void api_count_launch() { g_launches.fetch_add(1); }
+}  // namespace satgb
 
 extern "C" {
 
@@ -544,6 +590,13 @@ satgb_status satgb_sat_ex(const satgb_sat_desc* d, satgb_stream stream) {
   if (!d) return fail(SATGB_ERR_INVALID_ARG, "null descriptor");
   return sat_single(d->in_t, d->out_t, d->mode, d->direction, d->d_in, d->in_pitch, d->d_out, d->out_pitch,
                     d->width, d->height, (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_sat_planes(const satgb_sat_desc* d, int64_t n_planes, int64_t in_plane_stride,
+                              int64_t out_plane_stride, satgb_stream stream) {
+  if (!d) return fail(SATGB_ERR_INVALID_ARG, "null descriptor");
+  return sat_single(d->in_t, d->out_t, d->mode, d->direction, d->d_in, d->in_pitch, d->d_out, d->out_pitch,
+                    d->width, d->height, (cudaStream_t)stream, -1, n_planes, in_plane_stride, out_plane_stride);
 }
 
 satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream) {
@@ -702,7 +755,7 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   long long base = 0;
   for (auto& c : keep) {
     ImageDesc d;
-    fill_image_desc(d, p->v, in_t, out_t, c.in, c.out, c.in_pitch, c.out_pitch, c.width, c.height, base);
+    fill_image_desc(d, p->v, in_t, out_t, c.in, c.out, c.in_pitch, c.out_pitch, c.width, c.height, base, 1, 0, 0);
     base += (long long)d.ntx * d.nty;
     table.push_back(d);
   }

@@ -160,7 +160,7 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
   if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
 
   ImageDesc img;
-  fill_image_desc(img, v, d->in_t, d->out_t, d->d_in, d->d_out, d->in_pitch, d->out_pitch, d->width, d->height, 0);
+  fill_image_desc(img, v, d->in_t, d->out_t, d->d_in, d->d_out, d->in_pitch, d->out_pitch, d->width, d->height, 0, 1, 0, 0);
 
   SatParams P;
   std::memset(&P, 0, sizeof P);

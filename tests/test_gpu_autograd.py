@@ -1,0 +1,188 @@
+"""Multi-plane SATs, box filters and their autograd backward on the GPU.
+
+Plane stacks are integer-exact against the oracle plane by plane.  Box means
+and gradients are floating point (f32 through an f32 SAT) and are judged
+against float64 torch references with the tolerances written below:
+
+  box means        |m - m64| <= 4 * eps32 * max|S64| / area + 1e-7
+  gradients        |g - g64| <= 1e-4 * max(1, max|g64|)
+  central FD       |g - fd|  <= 1e-4 * max(1, max|fd|)   (FP64 loss, h = 1e-3)
+"""
+import numpy as np
+import pytest
+import torch
+
+import sat_gb300
+from sat_gb300 import autograd as AG
+from sat_gb300 import api
+from tests.util import bits, to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+EPS32 = float(np.finfo(np.float32).eps)
+
+
+def sat64(x: torch.Tensor) -> torch.Tensor:
+    return x.double().cumsum(-1).cumsum(-2)
+
+
+def box_means64(x: torch.Tensor, radii) -> torch.Tensor:
+    """Clipped box means in float64 by the four-corner rule on a zero-padded
+    SAT (differentiable, for reference gradients)."""
+    H, W = x.shape[-2:]
+    S = torch.nn.functional.pad(sat64(x), (1, 0, 1, 0))  # S[y+1, x+1] = SAT(y, x)
+    ys = torch.arange(H, device=x.device)
+    xs = torch.arange(W, device=x.device)
+    outs = []
+    for r in radii:
+        ya, yb = (ys - r).clamp(min=0), (ys + r).clamp(max=H - 1)
+        xa, xb = (xs - r).clamp(min=0), (xs + r).clamp(max=W - 1)
+        s = (S[..., yb + 1, :][..., xb + 1] - S[..., ya, :][..., xb + 1]
+             - S[..., yb + 1, :][..., xa] + S[..., ya, :][..., xa])
+        area = ((yb - ya + 1).double()[:, None] * (xb - xa + 1).double()[None, :])
+        outs.append(s / area)
+    return torch.stack(outs, dim=-3)
+
+
+def test_planes_integer_exact(cuda, oracle):
+    n, c, h, w = 2, 3, 131, 277
+    a = oracle.gen("u8", 11, (n * c * h, w)).reshape(n, c, h, w)
+    x = to_dev(a)
+    out = to_np(sat_gb300.sat(x, torch.uint32))
+    for i in range(n):
+        for j in range(c):
+            ref = oracle.sat_serial(a[i, j], np.uint32)
+            assert np.array_equal(bits(out[i, j]), bits(ref)), (i, j)
+
+
+def test_planes_pitched_and_reverse(cuda, oracle):
+    """Planes whose rows are a slice of wider rows (pitch > width), forward
+    and reverse, f32 -> f32 and u8 -> u32."""
+    p, h, w, pitch = 5, 97, 200, 256
+    a = oracle.gen("u8", 12, (p * h, w)).reshape(p, h, w)
+    base = torch.zeros((p, h, pitch), dtype=torch.uint8, device=cuda)
+    base[..., :w] = to_dev(a)
+    x = base[..., :w]
+    for rev in (False, True):
+        out = to_np(sat_gb300.sat(x, torch.uint32, reverse=rev))
+        for i in range(p):
+            ref = oracle.sat_reverse(a[i], np.uint32) if rev else oracle.sat_serial(a[i], np.uint32)
+            assert np.array_equal(bits(out[i]), bits(ref)), (i, rev)
+    af = oracle.gen("f32n", 13, (p * h, w)).astype(np.float32).reshape(p, h, w)
+    outf = to_np(sat_gb300.sat(to_dev(af), torch.float32))
+    for i in range(p):
+        ref = oracle.sat_fp64(af[i])
+        den = oracle.sat_fp64(af[i], absval=True)
+        assert np.max(np.abs(outf[i] - ref) / np.maximum(den, 1e-30)) <= 1e-5
+
+
+def test_planes_many_small(cuda, oracle):
+    """More planes than tiles per plane: 300 planes of 40 x 70."""
+    a = oracle.gen("u8", 14, (300 * 40, 70)).reshape(300, 40, 70)
+    out = to_np(sat_gb300.sat(to_dev(a), torch.uint32))
+    for i in (0, 1, 150, 299):
+        assert np.array_equal(bits(out[i]), bits(oracle.sat_serial(a[i], np.uint32))), i
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 37, 53), (2, 3, 64, 64), (1, 2, 5, 300)])
+def test_box_means_forward(cuda, shape):
+    g = torch.Generator(device="cpu").manual_seed(21)
+    x = torch.randn(shape, generator=g, dtype=torch.float32).to(cuda)
+    radii = (0, 1, 3, 40)  # 40 exceeds every side: the whole image
+    m = AG.box_filter_means(x, radii)
+    ref = box_means64(x, radii)
+    H, W = shape[-2:]
+    smax = float(sat64(x.abs()).max())
+    for k, r in enumerate(radii):
+        area_min = (min(r, H - 1) + 1) * (min(r, W - 1) + 1)
+        tol = 4 * EPS32 * smax / area_min + 1e-7
+        err = float((m[..., k, :, :].double() - ref[..., k, :, :]).abs().max())
+        assert err <= tol, (r, err, tol)
+
+
+def test_box_means_single_radius_matches_full_sum(cuda):
+    x = torch.rand((3, 17, 29), device=cuda)
+    m = AG.box_filter_means(x, (100,))
+    full = x.double().mean(dim=(-2, -1))
+    assert torch.allclose(m[:, 0].double(), full[:, None, None].expand(3, 17, 29), atol=1e-6)
+
+
+def _grads(x, radii, wts):
+    xg = x.clone().requires_grad_(True)
+    loss = (AG.box_filter_means(xg, radii) * wts).sum()
+    loss.backward()
+    x64 = x.double().clone().requires_grad_(True)
+    loss64 = (box_means64(x64, radii) * wts.double()).sum()
+    loss64.backward()
+    return xg.grad, x64.grad
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 64, 64), (1, 1, 33, 150), (1, 1, 1, 9)])
+def test_box_grad_vs_float64_cumsum(cuda, shape):
+    g = torch.Generator(device="cpu").manual_seed(22)
+    x = torch.randn(shape, generator=g).to(cuda)
+    radii = (3, 7, 15)
+    wts = torch.randn(shape[:-2] + (3,) + shape[-2:], generator=g).to(cuda)
+    gx, g64 = _grads(x, radii, wts)
+    tol = 1e-4 * max(1.0, float(g64.abs().max()))
+    assert float((gx.double() - g64).abs().max()) <= tol
+
+
+def test_box_grad_central_fd(cuda):
+    """64 x 64 crops: the kernel gradient against FP64 central differences
+    (h = 1e-3) of the FP64 loss at 24 random pixels."""
+    g = torch.Generator(device="cpu").manual_seed(23)
+    x = torch.randn((1, 3, 64, 64), generator=g).to(cuda)
+    radii = (3, 7, 15)
+    wts = torch.randn((1, 3, 3, 64, 64), generator=g).to(cuda)
+    xg = x.clone().requires_grad_(True)
+    (AG.box_filter_means(xg, radii) * wts).sum().backward()
+    grad = xg.grad.double()
+    x64 = x.double()
+    h = 1e-3
+    rng = np.random.default_rng(23)
+    pts = [(int(rng.integers(3)), int(rng.integers(64)), int(rng.integers(64))) for _ in range(20)]
+    pts += [(0, 0, 0), (1, 63, 63), (2, 0, 63), (0, 63, 0)]
+    fds, ours = [], []
+    for c, i, j in pts:
+        e = torch.zeros_like(x64)
+        e[0, c, i, j] = h
+        lp = float((box_means64(x64 + e, radii) * wts.double()).sum())
+        lm = float((box_means64(x64 - e, radii) * wts.double()).sum())
+        fds.append((lp - lm) / (2 * h))
+        ours.append(float(grad[0, c, i, j]))
+    fds, ours = np.array(fds), np.array(ours)
+    assert np.max(np.abs(fds - ours)) <= 1e-4 * max(1.0, np.max(np.abs(fds)))
+
+
+def test_sat_function_grad(cuda):
+    g = torch.Generator(device="cpu").manual_seed(24)
+    x = torch.randn((2, 45, 71), generator=g).to(cuda)
+    w = torch.randn((2, 45, 71), generator=g).to(cuda)
+    xg = x.clone().requires_grad_(True)
+    (AG.sat(xg) * w).sum().backward()
+    x64 = x.double().clone().requires_grad_(True)
+    (sat64(x64) * w.double()).sum().backward()
+    assert float((xg.grad.double() - x64.grad).abs().max()) <= 1e-4 * float(x64.grad.abs().max())
+
+
+def test_box_layer_module(cuda):
+    layer = AG.BoxFilter((1, 2))
+    x = torch.randn((2, 8, 8), device=cuda, requires_grad=True)
+    y = layer(x)
+    assert y.shape == (2, 2, 8, 8)
+    y.sum().backward()
+    assert x.grad is not None and x.grad.shape == x.shape
+
+
+def test_box_filter_rejects_bad_args(cuda):
+    x = torch.randn((4, 4), device=cuda)
+    s = api.sat(x)
+    with pytest.raises(sat_gb300.SatError):
+        api.box_means_from_sat(s, ())
+    with pytest.raises(sat_gb300.SatError):
+        api.box_means_from_sat(s, (1, 2, 3, 4, 5))
+    with pytest.raises(sat_gb300.SatError):
+        api.box_means_from_sat(s, (-1,))
+    with pytest.raises(sat_gb300.SatError):
+        api.box_means_from_sat(s.double(), (1,))

@@ -150,6 +150,37 @@ def test_pitched_unaligned_and_inplace(cuda, oracle):
     _check(oracle, f, to_np(x), np.float32)
 
 
+@pytest.mark.parametrize("pair", ["u8_u32", "u8_f64", "f32_f32", "f64_f64", "i8_i32"])
+def test_aligned_pitch_ragged_width(cuda, oracle, pair):
+    """16-byte aligned pitches with widths that end mid-chunk: the tensor maps
+    cover the whole 16-byte chunks and the row tails go by plain accesses.
+    The row padding (sentinel-filled) must stay untouched, forward and reverse."""
+    ti, to = oracle.PAIRS[pair]
+    ti, to = np.dtype(ti), np.dtype(to)
+    kind = {"u1": "u8", "i1": "i8", "f4": "f32u", "f8": "f64u"}[ti.str[1:]]
+    tin = {np.dtype(np.uint8): torch.uint8, np.dtype(np.int8): torch.int8,
+           np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}[ti]
+    tout = {np.dtype(np.uint32): torch.uint32, np.dtype(np.int32): torch.int32,
+            np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}[to]
+    for h, w in [(70, 17), (131, 555), (66, 1001), (40, 3), (257, 129)]:
+        a = oracle.gen(kind, 40 + w, (h, w)).astype(ti)
+        pin = -(-w * ti.itemsize // 64) * 64 // ti.itemsize + 16 // ti.itemsize
+        pout = -(-w * to.itemsize // 64) * 64 // to.itemsize + 16 // to.itemsize
+        src = empty_pitched(h, w, pin, tin)
+        src.copy_(to_dev(a))
+        fill = -1 if to.kind in "iu" else float("nan")
+        for rev in (False, True):
+            dst = empty_pitched(h, w, pout, tout, fill=fill)
+            sat_gb300.sat(src, tout, reverse=rev, out=dst)
+            _check(oracle, a, to_np(dst), to, reverse=rev)
+            pad = dst.as_strided((h, pout - w), (pout, 1), dst.storage_offset() + w)
+            padn = to_np(pad)
+            if to.kind in "iu":
+                assert np.all(bits(padn) == 0xFF), (h, w, rev)
+            else:
+                assert np.all(np.isnan(padn)), (h, w, rev)
+
+
 def test_back_to_back_calls_reuse_workspace(cuda, oracle):
     rng = np.random.default_rng(0)
     outs = []
