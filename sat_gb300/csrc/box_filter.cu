@@ -35,6 +35,7 @@ struct BoxArgs {
   int64_t sat_pitch, sat_plane;
   int nr;
   int r[SATGB_MAX_RADII];
+  float inv_full[SATGB_MAX_RADII]; // 1 / (2r + 1): the reciprocal window length away from the edges
   float* box[SATGB_MAX_RADII];
   int64_t box_pitch, box_plane;
 };
@@ -48,11 +49,15 @@ struct Win {
   int lo, hi;
   float inv;
 };
-__device__ __forceinline__ Win win(int i, int r, int n) {
+__device__ __forceinline__ Win win(int i, int r, int n, float inv_full) {
   Win w;
   w.lo = max(0, i - r);
   w.hi = min(n - 1, i + r);
-  w.inv = 1.0f / (float)(w.hi - w.lo + 1);
+  if (i - r >= 0 && i + r <= n - 1) {
+    w.inv = inv_full; // the whole window fits: the common case, no division
+  } else {
+    w.inv = 1.0f / (float)(w.hi - w.lo + 1);
+  }
   return w;
 }
 
@@ -66,13 +71,14 @@ __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constan
 #pragma unroll 1
   for (int i = 0; i < a.nr; ++i) {
     const int r = a.r[i];
-    const Win wx = win(x, r, W);
+    const float inv_full = a.inv_full[i];
+    const Win wx = win(x, r, W, inv_full);
     float* B = a.box[i] + pl * a.box_plane;
 #pragma unroll 4
     for (int k = 0; k < kRows; ++k) {
       const int y = ybase + k * kBY;
       if (y >= H) break;
-      const Win wy = win(y, r, H);
+      const Win wy = win(y, r, H, inv_full);
       const float* lo = S + (long long)(wy.lo - 1) * a.sat_pitch; // row ya-1 (unused when ya == 0)
       const float* hi = S + (long long)wy.hi * a.sat_pitch;
       float s = __ldg(hi + wx.hi);
@@ -89,12 +95,13 @@ __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constan
 
 // h(y,x) = g(y,x) / area(y,x) for radius r
 __device__ __forceinline__ float h_at(const float* g, long long pitch, int y, int x, int r, int H, int W) {
-  return __ldg(g + (long long)y * pitch + x) * (win(y, r, H).inv * win(x, r, W).inv);
+  return __ldg(g + (long long)y * pitch + x) / (float)((min(H - 1, y + r) - max(0, y - r) + 1) *
+                                                        (min(W - 1, x + r) - max(0, x - r) + 1));
 }
 
 // dS(p,q) for radius r on the last row or column, where the +1 index set is
 // a range: the general gather.
-__device__ float adjoint_edge(const float* g, long long pitch, int pr, int q, int r, int H, int W) {
+__device__ __noinline__ float adjoint_edge(const float* g, long long pitch, int pr, int q, int r, int H, int W) {
   int y0, y1, x0, x1;
   if (pr < H - 1) {
     y0 = y1 = pr - r;
@@ -126,55 +133,59 @@ __device__ float adjoint_edge(const float* g, long long pitch, int pr, int q, in
   return t;
 }
 
-__global__ void __launch_bounds__(kBX * kBY) box_bwd_kernel(const __grid_constant__ BoxArgs a) {
+__global__ void __launch_bounds__(kBX * kBY, 4) box_bwd_kernel(const __grid_constant__ BoxArgs a) {
   const int W = (int)a.w, H = (int)a.h;
   const int q = blockIdx.x * kBX + threadIdx.x;
   if (q >= W) return;
   const long long pl = blockIdx.z;
   const int ybase = blockIdx.y * (kBY * kRows) + threadIdx.y;
-  float acc[kRows];
+  const bool col_edge = q == W - 1;
+  // per radius: +h at column q - r, -h at column q + 1 + r (when inside),
+  // each with its reciprocal window width (0 marks a column outside)
+  float ixp[SATGB_MAX_RADII], ixm[SATGB_MAX_RADII];
 #pragma unroll
-  for (int k = 0; k < kRows; ++k) acc[k] = 0.f;
-#pragma unroll 1
-  for (int i = 0; i < a.nr; ++i) {
-    const int r = a.r[i];
-    const float* g = a.box[i] + pl * a.box_plane;
-    // interior columns: +h at x = q - r, -h at x = q + 1 + r (when inside)
-    const int xp = q - r, xm = q + 1 + r;
-    const bool hp = xp >= 0, hm = xm <= W - 1;
-    const float ixp = hp ? win(xp, r, W).inv : 0.f;
-    const float ixm = hm ? win(xm, r, W).inv : 0.f;
-    const bool col_edge = q == W - 1;
-#pragma unroll
-    for (int k = 0; k < kRows; ++k) {
-      const int pr = ybase + k * kBY;
-      if (pr >= H) break;
-      if (col_edge || pr == H - 1) {
-        acc[k] += adjoint_edge(g, a.box_pitch, pr, q, r, H, W);
-        continue;
-      }
-      const int yp = pr - r, ym = pr + 1 + r;
-      float t = 0.f;
-      if (yp >= 0) {
-        const float* row = g + (long long)yp * a.box_pitch;
-        float u = hp ? __ldg(row + xp) * ixp : 0.f;
-        if (hm) u -= __ldg(row + xm) * ixm;
-        t = u * win(yp, r, H).inv;
-      }
-      if (ym <= H - 1) {
-        const float* row = g + (long long)ym * a.box_pitch;
-        float u = hp ? __ldg(row + xp) * ixp : 0.f;
-        if (hm) u -= __ldg(row + xm) * ixm;
-        t -= u * win(ym, r, H).inv;
-      }
-      acc[k] += t;
+  for (int i = 0; i < SATGB_MAX_RADII; ++i) {
+    ixp[i] = ixm[i] = 0.f;
+    if (i < a.nr) {
+      const int r = a.r[i];
+      if (q - r >= 0) ixp[i] = win(q - r, r, W, a.inv_full[i]).inv;
+      if (q + 1 + r <= W - 1) ixm[i] = win(q + 1 + r, r, W, a.inv_full[i]).inv;
     }
   }
   float* dS = a.sat + pl * a.sat_plane;
-#pragma unroll
+#pragma unroll 1
   for (int k = 0; k < kRows; ++k) {
     const int pr = ybase + k * kBY;
-    if (pr < H) __stcs(dS + (long long)pr * a.sat_pitch + q, acc[k]);
+    if (pr >= H) break;
+    float acc = 0.f;
+    if (col_edge || pr == H - 1) {
+      for (int i = 0; i < a.nr; ++i)
+        acc += adjoint_edge(a.box[i] + pl * a.box_plane, a.box_pitch, pr, q, a.r[i], H, W);
+      __stcs(dS + (long long)pr * a.sat_pitch + q, acc);
+      continue;
+    }
+#pragma unroll
+    for (int i = 0; i < SATGB_MAX_RADII; ++i) {
+      if (i >= a.nr) break;
+      const int r = a.r[i];
+      const float* g = a.box[i] + pl * a.box_plane;
+      const int xp = q - r, xm = q + 1 + r, yp = pr - r, ym = pr + 1 + r;
+      float t = 0.f;
+      if (yp >= 0) {
+        const float* row = g + (long long)yp * a.box_pitch;
+        float u = ixp[i] != 0.f ? __ldg(row + xp) * ixp[i] : 0.f;
+        if (ixm[i] != 0.f) u -= __ldg(row + xm) * ixm[i];
+        t = u * win(yp, r, H, a.inv_full[i]).inv;
+      }
+      if (ym <= H - 1) {
+        const float* row = g + (long long)ym * a.box_pitch;
+        float u = ixp[i] != 0.f ? __ldg(row + xp) * ixp[i] : 0.f;
+        if (ixm[i] != 0.f) u -= __ldg(row + xm) * ixm[i];
+        t -= u * win(ym, r, H, a.inv_full[i]).inv;
+      }
+      acc += t;
+    }
+    __stcs(dS + (long long)pr * a.sat_pitch + q, acc);
   }
 }
 
@@ -210,12 +221,14 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
   a.box_plane = d->box_plane_stride;
   for (int i = 0; i < SATGB_MAX_RADII; ++i) {
     a.r[i] = 0;
+    a.inv_full[i] = 1.0f;
     a.box[i] = nullptr;
   }
   for (int i = 0; i < d->n_radii; ++i) {
     if (d->radius[i] < 0 || !d->d_box[i]) return SATGB_ERR_INVALID_ARG;
     if (((uintptr_t)d->d_box[i] % 4) != 0) return SATGB_ERR_MISALIGNED;
     a.r[i] = d->radius[i];
+    a.inv_full[i] = 1.0f / (float)(2 * (double)d->radius[i] + 1);
     a.box[i] = static_cast<float*>(d->d_box[i]);
   }
   return SATGB_OK;

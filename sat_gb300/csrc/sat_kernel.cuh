@@ -183,6 +183,54 @@ __device__ __forceinline__ void store_seg(TOut* p, bool vec, int nvalid, const T
   }
 }
 
+// Cold paths, kept out of line so the tile loop stays small: a thread moves
+// its own RPW x CPT block between global memory and its slots of the stage
+// (row stride TW elements).  fill: rows [0, rows) and columns [c0, nvalid)
+// come from global memory, columns below c0 are left as they are (TMA filled
+// them), everything else becomes zero.  drain: the block's valid part
+// (rows [0, rows), columns [c0, nvalid)) goes to global memory.
+template <class TIn, int CPT, int RPW, int TW>
+__device__ __noinline__ void stage_fill(TIn* sb, const TIn* g, long long pitch, int rows, int nvalid, int c0,
+                                        bool vec) {
+  for (int r = 0; r < RPW; ++r) {
+    TIn x[CPT];
+    if (c0 > 0) load_seg_smem<TIn, CPT>(sb + r * TW, x);
+    if (r < rows && nvalid > 0) {
+      if (vec && c0 == 0 && nvalid == CPT) {
+        load_seg<TIn, CPT>(g + r * pitch, true, CPT, x);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c)
+          if (c >= c0) x[c] = (c < nvalid) ? __ldcs(g + r * pitch + c) : TIn(0);
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < CPT; ++c)
+        if (c >= c0) x[c] = TIn(0);
+    }
+    RowSeg<TIn, CPT> seg;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) seg.u.e[c] = x[c];
+    *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = seg.u.v;
+  }
+}
+
+template <class TOut, int CPT, int RPW, int TW, bool REV>
+__device__ __noinline__ void stage_drain(const TOut* so, TOut* g, long long pitch, int rows, int nvalid, int c0,
+                                         bool vec) {
+  for (int r = 0; r < rows && r < RPW; ++r) {
+    TOut o[CPT];
+    load_seg_smem<TOut, CPT>(so + r * TW, o);
+    if (vec && c0 == 0 && nvalid == CPT) {
+      store_seg<TOut, CPT>(g + r * pitch, true, CPT, o);
+    } else {
+#pragma unroll
+      for (int c = 0; c < CPT; ++c)
+        if (c >= c0 && c < nvalid) __stcs(g + r * pitch + c, o[c]);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier / TMA / named-barrier helpers (inline PTX)
 // ---------------------------------------------------------------------------
@@ -331,8 +379,9 @@ __device__ __forceinline__ void diag_tile(long long k, int ntx, int nty, int& tx
 // that has published nothing yet, it reads the window again, now starting at
 // that predecessor.  So an inclusive value W tiles back is found in one round
 // trip as long as the tiles in between have published their aggregates, which
-// they do right after their local phase.  The first window is read when the
-// tile starts, overlapping the local phase.
+// they do right after their local phase.  The first window is read one local
+// phase ahead of its use (before the next tile's local phase), so that round
+// trip overlaps work and the values it sees are recent.
 template <class A>
 struct EarlyWin {
   static constexpr int W = Ar<A>::K == 1 ? 4 : 3;
@@ -470,7 +519,7 @@ struct TileShape {
 // stage `st` (TMA, or a bare arrive for images read from global memory).
 // Returns false once the tickets are exhausted (the stage then carries -1).
 template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES>
-__device__ __forceinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
+__device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
                                         long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
                                         unsigned long long* s_full) {
   const uint32_t bar = smem_u32(&s_full[st]);
@@ -614,7 +663,6 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   Tile nxt, cur;
   A E_nxt[RPW], E_cur[RPW];
   A agg_cur = AR::zero(); // this thread's element of the current tile's aggregate (column or row groups)
-  EarlyWin<A> win;        // look-back window of the current tile (columns, rows or the corner)
   const unsigned long long* lb_base = nullptr;
   long long lb_stride = 0;
   int lb_steps = 0;
@@ -643,29 +691,17 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     const TIn* gin = static_cast<const TIn*>(D.in) + (long long)nxt.p * D.in_plane + (y0 + warp * RPW) * D.in_pitch + xt;
     const bool vin = (flags & kInVec) && nvalid == CPT;
     const bool tail_in = tma && nvalid > 0 && xt + nvalid > D.tma_in_w;
+    if (!tma || tail_in) {
+      // no TMA for this image, or columns past the map (they arrived as zeros)
+      const long long rows = D.height - (y0 + warp * RPW);
+      const int c0 = tma ? (int)(D.tma_in_w - xt > 0 ? D.tma_in_w - xt : 0) : 0;
+      stage_fill<TIn, CPT, RPW, TW>(sb, gin, D.in_pitch, rows < 0 ? 0 : (rows > RPW ? RPW : (int)rows), nvalid, c0,
+                                    vin);
+    }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
       RowSeg<TIn, CPT> x;
-      if (tma) {
-        x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
-        if (tail_in && y0 + warp * RPW + r < D.height) {
-          // columns past the map arrived as zeros: load them and patch the stage
-#pragma unroll
-          for (int c = 0; c < CPT; ++c)
-            if (xt + c >= D.tma_in_w && c < nvalid) x.u.e[c] = gin[r * D.in_pitch + c];
-          *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = x.u.v;
-        }
-      } else {
-        // no TMA for this image: load from global memory and park the values in
-        // the stage for the output phase (each thread reads back only its own block)
-        if (y0 + warp * RPW + r < D.height && nvalid > 0) {
-          load_seg<TIn, CPT>(gin + r * D.in_pitch, vin, nvalid, x.u.e);
-        } else {
-#pragma unroll
-          for (int c = 0; c < CPT; ++c) x.u.e[c] = TIn(0);
-        }
-        *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = x.u.v;
-      }
+      x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
       A rs = AR::zero();
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
@@ -706,7 +742,6 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     for (int r = 0; r < RPW; ++r) E_nxt[r] = s_tr[warp][r][lane ^ r];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) s_colp[kk & 1][warp][c * 32 + lane] = colp[c];
-    if (!tma) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     return true;
   };
 
@@ -735,7 +770,6 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       lb_base = P.col_words + ((unsigned long long)t * TW + j) * K;
       lb_stride = (REV ? 1 : -1) * (long long)ntx * TW * K;
       lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
-      early_read<A>(win, lb_base, lb_stride, lb_steps);
     } else if (tid < TW + TH) {
       const int yy = tid - TW;
       const A ar = s_rowagg[yy];
@@ -745,33 +779,42 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       lb_base = P.row_words + ((unsigned long long)t * TH + yy) * K;
       lb_stride = (REV ? 1 : -1) * (long long)TH * K;
       lb_steps = REV ? (ntx - 1 - nxt.tx) : nxt.tx;
-      early_read<A>(win, lb_base, lb_stride, lb_steps);
     } else if (warp == CW && lane == 0) {
       lb_base = P.corner_words + (unsigned long long)t * K;
       lb_stride = (REV ? 1 : -1) * (long long)ntx * K;
       lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
-      early_read<A>(win, lb_base, lb_stride, lb_steps);
     }
   };
 
-  bool have = phase_a(0);
-  __syncthreads();
-  if (have) start_lookback(0);
-
-  for (int k = 0; have; ++k) {
-    const int st = k % S;
-    cur = nxt;
-#pragma unroll
-    for (int r = 0; r < RPW; ++r) E_cur[r] = E_nxt[r];
-    const A my_agg = agg_cur;
-    EarlyWin<A> my_win = win;
+  // iteration k = -1 only runs the local phase of tile 0 (one copy of each
+  // phase in the code keeps the loop small)
+  bool have = true;
+  for (int k = -1;; ++k) {
+    const int st = (k + S) % S;
+    A my_agg = AR::zero();
+    EarlyWin<A> my_win; // look-back window of the current tile (columns, rows or the corner)
     const unsigned long long* my_base = lb_base;
     const long long my_stride = lb_stride;
     const int my_steps = lb_steps;
+    if (k >= 0) {
+      if (!have) break;
+      cur = nxt;
+#pragma unroll
+      for (int r = 0; r < RPW; ++r) E_cur[r] = E_nxt[r];
+      my_agg = agg_cur;
+      // the current tile's first look-back window: read now, used after A(k+1),
+      // so the round trip overlaps the local phase of the next tile
+      if (tid < TW + TH || (warp == CW && lane == 0)) early_read<A>(my_win, my_base, my_stride, my_steps);
+    }
 
     // ---- A(k+1) ----------------------------------------------------------------
     const bool have_next = phase_a(k + 1);
     __syncthreads();
+    if (k < 0) {
+      if (have_next) start_lookback(0);
+      have = have_next;
+      continue;
+    }
 
     // ---- B: the next tile's aggregates out, the current tile's look-backs in ----
     const long long t = cur.t;
@@ -783,13 +826,16 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       pub_col = REV ? (cur.ty > 0) : (cur.ty < D.nty - 1);
     }
     if (have_next) start_lookback(k + 1);
+    // one look-back call site for the three roles (columns, rows, corner)
+    A got = AR::zero();
+    if (tid < TW + TH || (warp == CW && lane == 0)) got = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
     if (tid < TW) {
-      const A above = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+      const A above = got;
       if (pub_col && !stall) publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
       s_colabove[tid] = above;
     } else if (tid < TW + TH) {
       const int yy = tid - TW;
-      const A left = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+      const A left = got;
       if (pub_row && !stall) publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, AR::add(left, my_agg), tagI);
       s_rowleft[yy] = left;
       // scan of rowleft over this warp's 32 rows, in scan order; the group sum
@@ -825,7 +871,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       }
     } else if (warp == CW) {
       if (lane == 0) {
-        const A c = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+        const A c = got;
         vstore(&s_corner, c);
         __threadfence_block();
         if (atomicAdd(&s_cnt_corner, 1) == 1) {
@@ -917,28 +963,26 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
           top[c] = AR::add(top[c], run);
           o[c] = OutCvt<TOut, A>::out(top[c]);
         }
-        if (tma_out) {
-          union {
-            uint4 v;
-            TOut e[CPT];
-          } u;
+        union {
+          uint4 v;
+          TOut e[CPT];
+        } u;
 #pragma unroll
-          for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
-          *reinterpret_cast<uint4*>(so + r * TW) = u.v;
-          if (tail_out && y0 + warp * RPW + r < height) {
-            // columns past the map: plain stores
-#pragma unroll
-            for (int c = 0; c < CPT; ++c)
-              if (xt + c >= D.tma_out_w && c < nvalid) out[r * out_pitch + c] = o[c];
-          }
-        } else if (y0 + warp * RPW + r < height && nvalid > 0) {
-          store_seg<TOut, CPT>(out + r * out_pitch, vout, nvalid, o);
-        }
+        for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
+        *reinterpret_cast<uint4*>(so + r * TW) = u.v;
+      }
+      if (!tma_out || tail_out) {
+        // no TMA for this image, or columns past the map: plain stores
+        const long long rows = height - (y0 + warp * RPW);
+        const int c0 = tma_out ? (int)(D.tma_out_w - xt > 0 ? D.tma_out_w - xt : 0) : 0;
+        stage_drain<TOut, CPT, RPW, TW, REV>(so, out, out_pitch, rows < 0 ? 0 : (rows > RPW ? RPW : (int)rows),
+                                             nvalid, c0, vout);
       }
       // end of the tile: shared vectors may be reused; with TMA output one bulk
       // tensor store moves the tile out (clipped at the image edges) and drains
-      // while the CTA goes on with the next tiles
-      if (tma_out) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      // while the CTA goes on with the next tiles.  The stage is written by the
+      // generic proxy and next read or overwritten by TMA: order the two.
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
       if (tma_out && tid == PT) {
         const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[cur.img].tmap_out;

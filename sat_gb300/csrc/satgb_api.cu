@@ -439,6 +439,7 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
   P.corner_words = (unsigned long long*)(b + L.corner_off);
   P.wait_limit_ns = g_wait_limit_ns.load();
   P.stall_tile = g_stall_tile.load();
+
   cudaError_t e = v->launch(P, grid, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
   g_launches.fetch_add(1);
