@@ -3,6 +3,7 @@
 #include <atomic>
 
 #include "sat_kernel.cuh"
+#include "sat_kernel_r.cuh"
 #include "sat_registry.h"
 
 namespace satgb {
@@ -43,6 +44,42 @@ Variant make_variant(int in_t, int out_t, int mode, int cfg) {
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
+// The same three for sat_tile_kernel_r (inputs held in registers, several
+// CTAs per SM).
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+cudaError_t prepare_impl_r() {
+  using SH = TileShapeR<TIn, TOut, A, RPW, NW, MINB>;
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> done[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  e = cudaFuncSetAttribute(&sat_tile_kernel_r<TIn, TOut, A, REV, RPW, NW, MINB>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
+  return e;
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+cudaError_t launch_impl_r(const SatParams& p, int grid, cudaStream_t s) {
+  using SH = TileShapeR<TIn, TOut, A, RPW, NW, MINB>;
+  cudaError_t e = prepare_impl_r<TIn, TOut, A, REV, RPW, NW, MINB>();
+  if (e != cudaSuccess) return e;
+  sat_tile_kernel_r<TIn, TOut, A, REV, RPW, NW, MINB><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+Variant make_variant_r(int in_t, int out_t, int mode, int cfg) {
+  using SH = TileShapeR<TIn, TOut, A, RPW, NW, MINB>;
+  return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
+                 &launch_impl_r<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 &prepare_impl_r<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 (const void*)&sat_tile_kernel_r<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
+}
+
 }  // namespace satgb
 
 // dtype codes (satgb_dtype)
@@ -53,20 +90,21 @@ Variant make_variant(int in_t, int out_t, int mode, int cfg) {
 #define SG_F32 6
 #define SG_F64 7
 
-// every tile configuration, both directions (rows per warp, warps, CTAs per SM):
-//   0: 64-row tiles, 16 warps       1: 128-row tiles, 16 warps (64-row for
-//                                       8-byte accumulators: shared memory)
-//   2: 32-row tiles, 8 warps, 2 CTAs per SM     3: 32-row tiles, 16 warps
+// every tile configuration, both directions (kernel, rows per warp, warps,
+// CTAs per SM):
+//   0: registers, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
+//   1: pipelined, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
+//   2: pipelined, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
+//   3: registers, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
-#define SG_ALL(TIN, TOUT, A, IT, OT, MODE)                                            \
-  satgb::make_variant<TIN, TOUT, A, false, 4, 16, 1>(IT, OT, MODE, 0),                \
-      satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1), \
-      satgb::make_variant<TIN, TOUT, A, false, 4, 8, 2>(IT, OT, MODE, 2),             \
-      satgb::make_variant<TIN, TOUT, A, false, 2, 16, 1>(IT, OT, MODE, 3),            \
-      satgb::make_variant<TIN, TOUT, A, true, 4, 16, 1>(IT, OT, MODE, 0),             \
-      satgb::make_variant<TIN, TOUT, A, true, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),  \
-      satgb::make_variant<TIN, TOUT, A, true, 4, 8, 2>(IT, OT, MODE, 2),              \
-      satgb::make_variant<TIN, TOUT, A, true, 2, 16, 1>(IT, OT, MODE, 3)
+#define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
+#define SG_DIR(TIN, TOUT, A, IT, OT, MODE, REV)                                         \
+  satgb::make_variant_r<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 0),         \
+      satgb::make_variant<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),    \
+      satgb::make_variant<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 2),       \
+      satgb::make_variant_r<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 3)
+#define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
+  SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

@@ -102,7 +102,8 @@ struct SatParams {
 };
 
 // Pipeline depth.  A stage holds one tile from its TMA load until its TMA
-// store has read the results back out of it, so a CTA cycles through S
+// store has read the results back out of it (or, for the register kernel,
+// until the output phase has read the input), so a CTA cycles through S
 // stages: as many as fit in its share of the SM's 227 KB of shared memory
 // (CTAS CTAs per SM) next to its static shared memory, between 2 and 6.
 template <int STAGE_BYTES, int STATIC_BYTES, int CTAS>
@@ -509,25 +510,27 @@ struct TileShape {
   static constexpr int IN_BYTES = TH * TW * (int)sizeof(TIn); // what the TMA load brings
   static constexpr int STAGE_BYTES = TH * TW * (int)(sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
   // static shared memory of the kernel (s_tr, s_colp, the vectors), roughly
-  static constexpr int STATIC_BYTES = (NW * RPW * 32 + 2 * NW * TW + 3 * TH + TW) * (int)sizeof(A) + 512;
+  // rows per transpose pass: two passes when two CTAs share an SM, to halve the scratch
+  static constexpr int RP = (CTAS == 2 && RPW == 8) ? 4 : RPW;
+  static constexpr int STATIC_BYTES = (NW * RP * 32 + 2 * NW * TW + 4 * TH + 2 * NW + TW) * (int)sizeof(A) + 256;
   static constexpr int S = Stages<STAGE_BYTES, STATIC_BYTES, CTAS>::value;
   static constexpr int DYN_SMEM = S * STAGE_BYTES;
   static constexpr int THREADS = NW * 32;
 };
 
-// Takes ticket `tk`, maps it to a tile and starts its input on its way into
-// stage `st` (TMA, or a bare arrive for images read from global memory).
-// Returns false once the tickets are exhausted (the stage then carries -1).
-template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES>
-__device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
-                                        long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
-                                        unsigned long long* s_full) {
-  const uint32_t bar = smem_u32(&s_full[st]);
-  if ((long long)tk >= P.n_tiles) {
-    s_tile[st] = -1;
-    mbar_arrive(bar);
-    return false;
-  }
+// A ticket mapped to its tile (t = -1: the tickets are exhausted).
+struct TilePlan {
+  long long t; // spatial tile index (status words)
+  int tx, ty, img, pl;
+};
+
+// Maps ticket `tk` to its tile.
+template <bool REV>
+__device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long long tk) {
+  TilePlan tp;
+  tp.t = -1;
+  tp.tx = tp.ty = tp.img = tp.pl = 0;
+  if ((long long)tk >= P.n_tiles) return tp;
   const long long q = REV ? (P.n_tiles - 1 - (long long)tk) : (long long)tk;
   int img = 0;
   if (P.n_images > 1) {
@@ -546,18 +549,50 @@ __device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, 
   const long long pl = local / D->tiles_per_plane;
   int tx, ty;
   diag_tile(local - pl * D->tiles_per_plane, ntx, nty, tx, ty);
-  s_tile[st] = D->tile_base + pl * D->tiles_per_plane + (long long)ty * ntx + tx;
-  s_img[st] = img;
-  s_tx[st] = tx;
-  s_ty[st] = ty;
-  s_pl[st] = (int)pl;
+  tp.t = D->tile_base + pl * D->tiles_per_plane + (long long)ty * ntx + tx;
+  tp.tx = tx;
+  tp.ty = ty;
+  tp.img = img;
+  tp.pl = (int)pl;
+  return tp;
+}
+
+// Publishes a planned tile to the CTA (shared tile info of stage `st`) and
+// starts its input on its way into the stage (TMA, or a bare arrive for
+// images read from global memory; a bare arrive with tile -1 at the end).
+template <class TIn, int TW, int TH, int STAGE_BYTES>
+__device__ __forceinline__ void issue_tile(const SatParams& P, const TilePlan& tp, int st, TIn* stage_ptr,
+                                           long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
+                                           unsigned long long* s_full) {
+  const uint32_t bar = smem_u32(&s_full[st]);
+  s_tile[st] = tp.t;
+  s_img[st] = tp.img;
+  s_tx[st] = tp.tx;
+  s_ty[st] = tp.ty;
+  s_pl[st] = tp.pl;
+  if (tp.t < 0) {
+    mbar_arrive(bar);
+    return;
+  }
+  const ImageDesc* D = (P.n_images == 1) ? &P.img0 : &P.images[tp.img];
   if (D->flags & kInTma) {
     mbar_arrive_expect_tx(bar, (uint32_t)STAGE_BYTES);
-    tma_load_3d(smem_u32(stage_ptr), &D->tmap_in, tx * TW, ty * TH, (int)pl, bar);
+    tma_load_3d(smem_u32(stage_ptr), &D->tmap_in, tp.tx * TW, tp.ty * TH, tp.pl, bar);
   } else {
     mbar_arrive(bar);
   }
-  return true;
+}
+
+// Takes ticket `tk`, maps it to a tile and starts its input on its way into
+// stage `st`.  Returns false once the tickets are exhausted (the stage then
+// carries -1).
+template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES>
+__device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
+                                        long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
+                                        unsigned long long* s_full) {
+  const TilePlan tp = plan_tile<REV>(P, tk);
+  issue_tile<TIn, TW, TH, STAGE_BYTES>(P, tp, st, stage_ptr, s_tile, s_img, s_tx, s_ty, s_pl, s_full);
+  return tp.t >= 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -604,8 +639,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   constexpr int CW = (TW + TH) / 32; // corner warp
   constexpr int PT = NC - 1;         // producer thread (in the last warp, never the corner warp)
   static_assert(CW < NW - 1, "corner warp and producer warp differ");
-  constexpr int LPR = 32 / RPW;      // transpose-scan: lanes per row ...
-  constexpr int CH = RPW;            // ... and values per lane
+  constexpr int RP = SH::RP;         // rows per transpose pass
+  constexpr int LPR = 32 / RP;       // transpose-scan: lanes per row ...
+  constexpr int CH = RP;             // ... and values per lane
   constexpr int K = Ar<A>::K;
   constexpr bool WIDEN = sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
   using AR = Ar<A>;
@@ -613,15 +649,17 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   extern __shared__ __align__(128) unsigned char dsmem[];
   TIn* stages = reinterpret_cast<TIn*>(dsmem);
 
-  __shared__ A s_tr[NW][RPW][32];   // per-warp transpose scratch (index lane ^ row: conflict free)
+  __shared__ A s_tr[NW][RP][32];    // per-warp transpose scratch (index lane ^ row: conflict free)
   __shared__ A s_colp[2][NW][TW];   // per warp: raw column partials (by slot); then the exclusive prefix over warps
   __shared__ A s_rowagg[TH];        // row totals of the tile in the local phase
-  __shared__ A s_rowleft[TH];       // row look-back result of the tile in the output phase
-  __shared__ A s_RL[TH];            // its scan over each 32-row group of the tile's rows
-  __shared__ A s_rlw[TH / 32];      // per 32-row group: the sum of rowleft
+  // row look-back results, by tile parity: tile k+1's are made while tile k's are used
+  __shared__ A s_rowleft[2][TH];    // rowleft of each row
+  __shared__ A s_RLw[2][NW];        // per warp: the scan over its 32-row group of rowleft, at the row before the warp
+  __shared__ A s_rlw[2][TH / 32];   // per 32-row group: the sum of rowleft
   __shared__ A s_colabove[TW];      // its column look-back result (by slot)
-  __shared__ A s_corner, s_u;
-  __shared__ int s_cnt_row, s_cnt_corner; // arrivals of the row warps / of {rows, corner}
+  __shared__ A s_corner;
+  __shared__ A s_u[2];              // u = sum of rowleft (the corner aggregate), by tile parity
+  __shared__ int s_cnt_row;         // arrivals of the row warps
   __shared__ long long s_tile[S];   // spatial tile index per stage (-1: no more tiles)
   __shared__ int s_img[S];
   __shared__ int s_tx[S], s_ty[S], s_pl[S];
@@ -635,10 +673,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   const uint32_t tagI = make_tag(epoch, kStateInc);
 
   unsigned long long pending = 0; // producer thread: the next ticket, fetched a tile ahead
-  bool producing = true;
+  bool producing = true;          // producer thread: tickets not yet exhausted
   if (tid == 0) {
     s_cnt_row = 0;
-    s_cnt_corner = 0;
   }
   if (tid == PT) {
 #pragma unroll
@@ -697,6 +734,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       const int c0 = tma ? (int)(D.tma_in_w - xt > 0 ? D.tma_in_w - xt : 0) : 0;
       stage_fill<TIn, CPT, RPW, TW>(sb, gin, D.in_pitch, rows < 0 ? 0 : (rows > RPW ? RPW : (int)rows), nvalid, c0,
                                     vin);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); // before TMA refills the stage
     }
 #pragma unroll
     for (int r = 0; r < RPW; ++r) {
@@ -711,35 +749,40 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       }
       rowp[r] = rs;
     }
-    // row partials -> exclusive prefix over the lanes (E) and the row totals
+    // row partials -> exclusive prefix over the lanes (E) and the row totals,
+    // RP rows per pass through the transpose scratch
 #pragma unroll
-    for (int r = 0; r < RPW; ++r) s_tr[warp][r][lane ^ r] = rowp[r];
-    __syncwarp();
-    {
-      const int r = lane / LPR, q = lane % LPR;
-      A tot = AR::zero();
+    for (int h = 0; h < RPW / RP; ++h) {
 #pragma unroll
-      for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][(q * CH + (REV ? CH - 1 - i : i)) ^ r]);
-      A incl = tot;
+      for (int r = 0; r < RP; ++r) s_tr[warp][r][lane ^ r] = rowp[h * RP + r];
+      __syncwarp();
+      {
+        const int r = lane / LPR, q = lane % LPR;
+        A tot = AR::zero();
 #pragma unroll
-      for (int d = 1; d < LPR; d <<= 1) {
-        const A o = REV ? AR::shfl_down(incl, d, LPR) : AR::shfl_up(incl, d, LPR);
-        if (REV ? (q + d < LPR) : (q >= d)) incl = AR::add(o, incl);
+        for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][(q * CH + (REV ? CH - 1 - i : i)) ^ r]);
+        A incl = tot;
+#pragma unroll
+        for (int d = 1; d < LPR; d <<= 1) {
+          const A o = REV ? AR::shfl_down(incl, d, LPR) : AR::shfl_up(incl, d, LPR);
+          if (REV ? (q + d < LPR) : (q >= d)) incl = AR::add(o, incl);
+        }
+        A ex = REV ? AR::shfl_down(incl, 1, LPR) : AR::shfl_up(incl, 1, LPR);
+        if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          const int idx = (q * CH + (REV ? CH - 1 - i : i)) ^ r;
+          const A vv = s_tr[warp][r][idx];
+          s_tr[warp][r][idx] = ex;
+          ex = AR::add(ex, vv);
+        }
+        if (q == (REV ? 0 : LPR - 1)) s_rowagg[warp * RPW + h * RP + r] = incl;
       }
-      A ex = REV ? AR::shfl_down(incl, 1, LPR) : AR::shfl_up(incl, 1, LPR);
-      if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
+      __syncwarp();
 #pragma unroll
-      for (int i = 0; i < CH; ++i) {
-        const int idx = (q * CH + (REV ? CH - 1 - i : i)) ^ r;
-        const A vv = s_tr[warp][r][idx];
-        s_tr[warp][r][idx] = ex;
-        ex = AR::add(ex, vv);
-      }
-      if (q == (REV ? 0 : LPR - 1)) s_rowagg[warp * RPW + r] = incl;
+      for (int r = 0; r < RP; ++r) E_nxt[h * RP + r] = s_tr[warp][r][lane ^ r];
+      if (RPW / RP > 1) __syncwarp();
     }
-    __syncwarp();
-#pragma unroll
-    for (int r = 0; r < RPW; ++r) E_nxt[r] = s_tr[warp][r][lane ^ r];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) s_colp[kk & 1][warp][c * 32 + lane] = colp[c];
     return true;
@@ -772,13 +815,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
     } else if (tid < TW + TH) {
       const int yy = tid - TW;
-      const A ar = s_rowagg[yy];
       if ((REV ? (nxt.tx > 0) : (nxt.tx < ntx - 1)) && !stall)
-        publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, ar, tagA);
-      agg_cur = ar;
-      lb_base = P.row_words + ((unsigned long long)t * TH + yy) * K;
-      lb_stride = (REV ? 1 : -1) * (long long)TH * K;
-      lb_steps = REV ? (ntx - 1 - nxt.tx) : nxt.tx;
+        publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, s_rowagg[yy], tagA);
     } else if (warp == CW && lane == 0) {
       lb_base = P.corner_words + (unsigned long long)t * K;
       lb_stride = (REV ? 1 : -1) * (long long)ntx * K;
@@ -802,42 +840,71 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
       for (int r = 0; r < RPW; ++r) E_cur[r] = E_nxt[r];
       my_agg = agg_cur;
-      // the current tile's first look-back window: read now, used after A(k+1),
-      // so the round trip overlaps the local phase of the next tile
-      if (tid < TW + TH || (warp == CW && lane == 0)) early_read<A>(my_win, my_base, my_stride, my_steps);
+      // the current tile's first column / corner look-back window: read now,
+      // used after A(k+1), so the round trip overlaps the local phase
+      if (tid < TW || (warp == CW && lane == 0)) early_read<A>(my_win, my_base, my_stride, my_steps);
+    }
+    // Row threads run the row look-back of the NEXT tile (k+1) in this
+    // iteration, right after its local phase: its u (the corner aggregate)
+    // then goes out without waiting for this CTA's corner of tile k.
+    long long rt = -1;
+    int rtx = 0, rty = 0, rntx = 1, rnty = 1;
+    if (tid >= TW && tid < TW + TH) {
+      const int sn = (k + 1) % S; // tile k+1's stage: filled at least one iteration ago
+      rt = s_tile[sn];
+      if (rt >= 0) {
+        rtx = s_tx[sn];
+        rty = s_ty[sn];
+        const ImageView Dn = image_view(P, s_img[sn]);
+        rntx = Dn.ntx;
+        rnty = Dn.nty;
+        my_base = P.row_words + ((unsigned long long)rt * TH + (tid - TW)) * K;
+        early_read<A>(my_win, my_base, (REV ? 1 : -1) * (long long)TH * K, REV ? (rntx - 1 - rtx) : rtx);
+      }
     }
 
     // ---- A(k+1) ----------------------------------------------------------------
     const bool have_next = phase_a(k + 1);
     __syncthreads();
-    if (k < 0) {
-      if (have_next) start_lookback(0);
-      have = have_next;
-      continue;
-    }
 
-    // ---- B: the next tile's aggregates out, the current tile's look-backs in ----
-    const long long t = cur.t;
+    // ---- B: the next tile's aggregates and row look-back, the current tile's
+    //      column and corner look-backs ------------------------------------------
+    const bool has_cur = k >= 0;
+    const long long t = has_cur ? cur.t : -1;
     const bool stall = (t == P.stall_tile);
-    bool pub_row, pub_col;
-    {
+    bool pub_col = false;
+    if (has_cur) {
       const ImageView D = image_view(P, cur.img);
-      pub_row = REV ? (cur.tx > 0) : (cur.tx < D.ntx - 1);
       pub_col = REV ? (cur.ty > 0) : (cur.ty < D.nty - 1);
     }
     if (have_next) start_lookback(k + 1);
     // one look-back call site for the three roles (columns, rows, corner)
     A got = AR::zero();
-    if (tid < TW + TH || (warp == CW && lane == 0)) got = resolve<A>(my_win, my_base, my_stride, my_steps, tagA, tagI, P, t);
+    const bool lb_row = tid >= TW && tid < TW + TH && rt >= 0;
+    const bool lb_cur = has_cur && (tid < TW || (warp == CW && lane == 0));
+    if (lb_row || lb_cur) {
+      const long long stride = lb_row ? (REV ? 1 : -1) * (long long)TH * K : my_stride;
+      const int steps = lb_row ? (REV ? (rntx - 1 - rtx) : rtx) : my_steps;
+      got = resolve<A>(my_win, my_base, stride, steps, tagA, tagI, P, lb_row ? rt : t);
+    }
     if (tid < TW) {
-      const A above = got;
-      if (pub_col && !stall) publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
-      s_colabove[tid] = above;
+      if (!has_cur) {
+        // nothing to do for the columns before the first tile
+      } else {
+        const A above = got;
+        if (pub_col && !stall)
+          publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
+        s_colabove[tid] = above;
+      }
     } else if (tid < TW + TH) {
+      if (rt >= 0) {
       const int yy = tid - TW;
+      const int nb = (k + 1) & 1;
+      const bool rstall = (rt == P.stall_tile);
       const A left = got;
-      if (pub_row && !stall) publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, AR::add(left, my_agg), tagI);
-      s_rowleft[yy] = left;
+      if ((REV ? (rtx > 0) : (rtx < rntx - 1)) && !rstall)
+        publish<A>(P.row_words + ((unsigned long long)rt * TH + yy) * K, AR::add(left, s_rowagg[yy]), tagI);
+      s_rowleft[nb][yy] = left;
       // scan of rowleft over this warp's 32 rows, in scan order; the group sum
       A incl = left;
 #pragma unroll
@@ -845,44 +912,34 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         const A o = REV ? AR::shfl_down(incl, d) : AR::shfl_up(incl, d);
         if (REV ? (lane + d < 32) : (lane >= d)) incl = AR::add(o, incl);
       }
-      s_RL[yy] = incl;
-      if (lane == (REV ? 0 : 31)) s_rlw[yy / 32] = incl;
+      if (REV ? (yy % RPW == 0 && yy > 0) : ((yy + 1) % RPW == 0 && yy + 1 < TH))
+        s_RLw[nb][REV ? yy / RPW - 1 : (yy + 1) / RPW] = incl;
+      if (lane == (REV ? 0 : 31)) s_rlw[nb][yy / 32] = incl;
       __syncwarp();
       if (lane == 0) {
-        // the last row warp to get here publishes u = sum of rowleft, the corner
-        // aggregate; the later of it and the corner warp publishes corner + u
+        // the last row warp to get here forms u = sum of rowleft and publishes it
+        // as the next tile's corner aggregate
         __threadfence_block();
         if (atomicAdd(&s_cnt_row, 1) == TH / 32 - 1) {
           __threadfence_block();
           s_cnt_row = 0;
           A u = AR::zero();
 #pragma unroll
-          for (int g = 0; g < TH / 32; ++g) u = AR::add(u, vload(&s_rlw[g]));
-          vstore(&s_u, u);
-          unsigned long long* cw = P.corner_words + (unsigned long long)t * K;
-          if (pub_col && !stall) publish<A>(cw, u, tagA);
-          __threadfence_block();
-          if (atomicAdd(&s_cnt_corner, 1) == 1) {
-            __threadfence_block();
-            s_cnt_corner = 0;
-            if (pub_col && !stall) publish<A>(cw, AR::add(vload(&s_corner), u), tagI);
-          }
+          for (int g = 0; g < TH / 32; ++g) u = AR::add(u, vload(&s_rlw[nb][g]));
+          s_u[nb] = u;
+          if ((REV ? (rty > 0) : (rty < rnty - 1)) && !rstall)
+            publish<A>(P.corner_words + (unsigned long long)rt * K, u, tagA);
         }
+      }
       }
     } else if (warp == CW) {
-      if (lane == 0) {
-        const A c = got;
-        vstore(&s_corner, c);
-        __threadfence_block();
-        if (atomicAdd(&s_cnt_corner, 1) == 1) {
-          __threadfence_block();
-          s_cnt_corner = 0;
-          if (pub_col && !stall)
-            publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(c, vload(&s_u)),
-                       tagI);
-        }
+      if (lane == 0 && has_cur) {
+        // corner of tile k; its u was formed in the previous iteration
+        s_corner = got;
+        if (pub_col && !stall)
+          publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(got, s_u[k & 1]), tagI);
       }
-    } else if (tid == PT && producing) {
+    } else if (tid == PT && producing && has_cur) {
       // tile k+S-1 into the stage whose store (tile k-1) has finished reading it
       const int ps = (st + S - 1) % S;
       bulk_wait_read_all();
@@ -891,12 +948,15 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
     }
     __syncthreads();
+    if (!has_cur) {
+      have = have_next;
+      continue;
+    }
 
     // ---- D(k): scan with the carries injected, results out ---------------------
     {
       const ImageView D = image_view(P, cur.img);
       const uint32_t flags = D.flags;
-      const bool tma_out = flags & kOutTma;
       const long long x0 = (long long)cur.tx * TW, y0 = (long long)cur.ty * TH;
       const long long xt = x0 + (long long)lane * CPT;
       const long long rem = D.width - xt;
@@ -909,10 +969,10 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         if (has_prev) {
           // RL of the row just outside the warp: its group's scan plus the groups before it
           const int yp = REV ? (warp + 1) * RPW : warp * RPW - 1;
-          rl_prev = s_RL[yp];
+          rl_prev = s_RLw[k & 1][warp];
 #pragma unroll
           for (int g = 0; g < TH / 32; ++g)
-            if (REV ? (g > yp / 32) : (g < yp / 32)) rl_prev = AR::add(s_rlw[g], rl_prev);
+            if (REV ? (g > yp / 32) : (g < yp / 32)) rl_prev = AR::add(s_rlw[k & 1][g], rl_prev);
         }
         A cp[CPT];
 #pragma unroll
@@ -935,6 +995,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       }
       TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
       TOut* so = reinterpret_cast<TOut*>(stages + st * STAGE_ELEMS) + (warp * RPW) * TW + lane * CPT;
+      const bool tma_out = flags & kOutTma;
       RowSeg<TIn, CPT> raw[WIDEN ? RPW : 1];
       if (WIDEN) {
         // wider outputs overwrite other threads' inputs: read all inputs first
@@ -954,22 +1015,19 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         RowSeg<TIn, CPT> x;
         if (WIDEN) x = raw[WIDEN ? r : 0];
         else x.u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
-        A run = AR::add(E_cur[r], s_rowleft[warp * RPW + r]);
-        TOut o[CPT];
+        A run = AR::add(E_cur[r], s_rowleft[k & 1][warp * RPW + r]);
+        union {
+          uint4 v;
+          TOut e[CPT];
+        } o;
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
           run = AR::add(run, Cvt<A, TIn>::in(x.u.e[c]));
           top[c] = AR::add(top[c], run);
-          o[c] = OutCvt<TOut, A>::out(top[c]);
+          o.e[c] = OutCvt<TOut, A>::out(top[c]);
         }
-        union {
-          uint4 v;
-          TOut e[CPT];
-        } u;
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
-        *reinterpret_cast<uint4*>(so + r * TW) = u.v;
+        *reinterpret_cast<uint4*>(so + r * TW) = o.v;
       }
       if (!tma_out || tail_out) {
         // no TMA for this image, or columns past the map: plain stores
