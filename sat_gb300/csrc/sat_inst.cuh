@@ -4,6 +4,7 @@
 
 #include "sat_kernel.cuh"
 #include "sat_kernel_r.cuh"
+#include "sat_kernel_ws.cuh"
 #include "sat_registry.h"
 
 namespace satgb {
@@ -80,6 +81,42 @@ Variant make_variant_r(int in_t, int out_t, int mode, int cfg) {
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
+// The same three for sat_tile_kernel_ws (warp-specialized; NWC compute warps
+// plus three role warps, one CTA per SM).
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+cudaError_t prepare_impl_ws() {
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> done[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  e = cudaFuncSetAttribute(&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
+  return e;
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+cudaError_t launch_impl_ws(const SatParams& p, int grid, cudaStream_t s) {
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+  cudaError_t e = prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC>();
+  if (e != cudaSuccess) return e;
+  sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+  return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
+                 &launch_impl_ws<TIn, TOut, A, REV, RPW, NWC>,
+                 &prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC>,
+                 (const void*)&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC>,
+                 SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
+}
+
 }  // namespace satgb
 
 // dtype codes (satgb_dtype)
@@ -92,14 +129,17 @@ Variant make_variant_r(int in_t, int out_t, int mode, int cfg) {
 
 // every tile configuration, both directions (kernel, rows per warp, warps,
 // CTAs per SM):
-//   0: registers, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
+//   0: warp-specialized, 64-row tiles, 16 compute warps (8 for 8-byte
+//      accumulators) + column, row and store warps
 //   1: pipelined, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
 //   2: pipelined, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
 //   3: registers, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
+#define SG_WS_RPW(A) (sizeof(A) == 8 ? 8 : 4)  /* 64-row tiles either way: */
+#define SG_WS_NWC(A) (sizeof(A) == 8 ? 8 : 16) /* 8-byte accumulators need the registers of fewer warps */
 #define SG_DIR(TIN, TOUT, A, IT, OT, MODE, REV)                                         \
-  satgb::make_variant_r<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 0),         \
+  satgb::make_variant_ws<TIN, TOUT, A, REV, SG_WS_RPW(A), SG_WS_NWC(A)>(IT, OT, MODE, 0), \
       satgb::make_variant<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),    \
       satgb::make_variant<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 2),       \
       satgb::make_variant_r<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 3)

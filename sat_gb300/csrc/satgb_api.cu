@@ -26,7 +26,7 @@
 namespace satgb {
 
 const TileConfig kConfigs[kNumConfigs] = {
-    {8, 8, "registers: 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs per SM"},
+    {4, 16, "warp-specialized: 64-row tiles, 16 compute warps, column/row look-back and store warps"},
     {8, 16, "pipelined: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
     {8, 8, "pipelined: 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs per SM"},
     {8, 16, "registers: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
@@ -397,19 +397,22 @@ int sms_of(int dev) {
 
 // Heuristic default when no tuning entry exists: the largest tiles that
 // still give every SM several of them.
-// Untuned choice.  4-byte accumulators: the 128-row pipelined tiles when
-// there are enough of them to fill the GPU a few times over, else the 64-row
-// two-CTA tiles.  8-byte accumulators (compensated f32, f64 outputs): the
-// 64-row register tiles for large images (their arithmetic dominates), else
-// the two-CTA tiles.
-int default_config(long long width, long long height, int sms, int out_sz, bool wide_acc) {
+// Untuned choice, from measurements on GB300 at 8192^2 (f32) and 4096^2 (f64).
+// 4-byte accumulators: the 128-row pipelined tiles when there are enough of
+// them to fill the GPU a few times over, else the 64-row two-CTA tiles.
+// Compensated f32: the 64-row register tiles (their arithmetic dominates).
+// f64 outputs (slow FP64 adds on GB300): the warp-specialized tiles, whose
+// compute warps never wait at a CTA barrier.
+int default_config(long long width, long long height, int sms, int out_sz, bool compensated) {
   const int cpt = 16 / out_sz;
   const long long tw = 32LL * cpt;
   const long long ntx = (width + tw - 1) / tw;
   const long long tiles128 = ntx * ((height + 127) / 128);
   sms = std::max(1, sms);
-  if (wide_acc) return tiles128 >= 8LL * sms ? 3 : 2;
-  return tiles128 >= 8LL * sms ? 1 : 2;
+  const bool large = tiles128 >= 8LL * sms;
+  if (out_sz == 8) return large ? 0 : 2;
+  if (compensated) return large ? 3 : 2;
+  return large ? 1 : 2;
 }
 
 int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, long long h, int dev) {
@@ -418,7 +421,7 @@ int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, lo
   const int sms = sms_of(dev);
   auto it = g_tune.find(TuneKey(in_t, out_t, mode, dir, log2_bucket(w), log2_bucket(h), sms));
   if (it != g_tune.end()) return it->second;
-  return default_config(w, h, sms, (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED || out_t == SATGB_F64);
+  return default_config(w, h, sms, (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED);
 }
 
 satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const ImageDesc& img0,
