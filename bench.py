@@ -523,12 +523,15 @@ def run_workload(args):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream()
     if args.case in ("batch512", "batch512_packed"):
+        if args.config >= 0:
+            sat_gb300.set_config(args.config)
         xs, ys, nbytes = build_batch(dev, pitched=args.case == "batch512")
         plan = sat_gb300.BatchPlan(xs, ys, stream=stream)
         _, per = _time_steps(lambda: plan.exec(stream), args.steps, args.warmup, stream, 0.0)
         plan.check(stream)
         med = statistics.median(per)
-        print(json.dumps({"case": args.case, "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1)}))
+        print(json.dumps({"case": args.case, "config": plan.info()["config"], "tiles": plan.info()["n_tiles"],
+                          "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1)}))
     elif args.case in ("box_fwd", "box_fwdbwd"):
         n = 8 if args.small else 64
         x, wts, radii = build_box(dev, n=n)

@@ -72,23 +72,35 @@ __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constan
   for (int i = 0; i < a.nr; ++i) {
     const int r = a.r[i];
     const float inv_full = a.inv_full[i];
+    const float inv2 = inv_full * inv_full;
     const Win wx = win(x, r, W, inv_full);
+    // columns whose window and the column before it lie inside the image
+    const bool xin = x - r - 1 >= 0 && x + r <= W - 1;
     float* B = a.box[i] + pl * a.box_plane;
 #pragma unroll 4
     for (int k = 0; k < kRows; ++k) {
       const int y = ybase + k * kBY;
       if (y >= H) break;
-      const Win wy = win(y, r, H, inv_full);
-      const float* lo = S + (long long)(wy.lo - 1) * a.sat_pitch; // row ya-1 (unused when ya == 0)
-      const float* hi = S + (long long)wy.hi * a.sat_pitch;
-      float s = __ldg(hi + wx.hi);
-      if (wx.lo > 0) s -= __ldg(hi + wx.lo - 1);
-      if (wy.lo > 0) {
-        float t = __ldg(lo + wx.hi);
-        if (wx.lo > 0) t -= __ldg(lo + wx.lo - 1);
-        s -= t;
+      float out;
+      if (xin && y - r - 1 >= 0 && y + r <= H - 1) {
+        // interior: four corners at fixed offsets, full window area
+        const float* hi = S + (long long)(y + r) * a.sat_pitch + x;
+        const float* lo = S + (long long)(y - r - 1) * a.sat_pitch + x;
+        out = ((__ldg(hi + r) - __ldg(hi - r - 1)) - (__ldg(lo + r) - __ldg(lo - r - 1))) * inv2;
+      } else {
+        const Win wy = win(y, r, H, inv_full);
+        const float* lo = S + (long long)(wy.lo - 1) * a.sat_pitch; // row ya-1 (unused when ya == 0)
+        const float* hi = S + (long long)wy.hi * a.sat_pitch;
+        float sum = __ldg(hi + wx.hi);
+        if (wx.lo > 0) sum -= __ldg(hi + wx.lo - 1);
+        if (wy.lo > 0) {
+          float t = __ldg(lo + wx.hi);
+          if (wx.lo > 0) t -= __ldg(lo + wx.lo - 1);
+          sum -= t;
+        }
+        out = sum * (wy.inv * wx.inv);
       }
-      __stcs(B + (long long)y * a.box_pitch + x, s * (wy.inv * wx.inv));
+      __stcs(B + (long long)y * a.box_pitch + x, out);
     }
   }
 }
@@ -153,7 +165,7 @@ __global__ void __launch_bounds__(kBX * kBY, 4) box_bwd_kernel(const __grid_cons
     }
   }
   float* dS = a.sat + pl * a.sat_plane;
-#pragma unroll 1
+#pragma unroll 2
   for (int k = 0; k < kRows; ++k) {
     const int pr = ybase + k * kBY;
     if (pr >= H) break;
@@ -170,6 +182,14 @@ __global__ void __launch_bounds__(kBX * kBY, 4) box_bwd_kernel(const __grid_cons
       const int r = a.r[i];
       const float* g = a.box[i] + pl * a.box_plane;
       const int xp = q - r, xm = q + 1 + r, yp = pr - r, ym = pr + 1 + r;
+      if (pr >= 2 * r && pr <= H - 2 - 2 * r && q >= 2 * r && q <= W - 2 - 2 * r) {
+        // interior: the four outputs with a corner here have whole windows
+        const float* rp = g + (long long)yp * a.box_pitch;
+        const float* rm = g + (long long)ym * a.box_pitch;
+        acc += ((__ldg(rp + xp) - __ldg(rp + xm)) - (__ldg(rm + xp) - __ldg(rm + xm))) *
+               (a.inv_full[i] * a.inv_full[i]);
+        continue;
+      }
       float t = 0.f;
       if (yp >= 0) {
         const float* row = g + (long long)yp * a.box_pitch;

@@ -755,7 +755,9 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   if (cfg < 0) {
     tune_load_locked();
     auto it = g_tune.find(TuneKey(in_t, out_t, mode, direction, log2_bucket(side), log2_bucket(side), sms_of(dev)));
-    cfg = it != g_tune.end() ? it->second : 0;
+    // untuned: the 64-row two-CTA tiles waste the least on small and uneven
+    // images; f64 outputs keep the warp-specialized tiles
+    cfg = it != g_tune.end() ? it->second : (dtype_size((satgb_dtype)out_t) == 8 ? 0 : 2);
   }
   p->v = find_variant(in_t, out_t, mode, direction, cfg);
   if (!p->v) p->v = find_variant(in_t, out_t, mode, direction, 0);
