@@ -86,7 +86,18 @@ def build(verbose: bool = False, force: bool = False, jobs: int = 0) -> str:
         tmp = target + ".tmp"
         run([nvcc, GENCODE, "-shared", "-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, target)
+    # the reference's command line (sat A S D0 D1 R) over the library
+    cli_src = os.path.join(CSRC, "sat_cli.cpp")
+    cli = cli_path()
+    if os.path.isfile(cli_src) and (force or _stale(cli, [cli_src, target])):
+        run([nvcc, "-O2", "-std=c++17", "-I", os.path.join(os.path.dirname(HERE), "include"), "-o", cli + ".tmp",
+             cli_src, "-L", OUT_DIR, "-lsatgb", "-lcudart", "-Xlinker", "-rpath,$ORIGIN"])
+        os.replace(cli + ".tmp", cli)
     return target
+
+
+def cli_path() -> str:
+    return os.path.join(OUT_DIR, "sat")
 
 
 if __name__ == "__main__":

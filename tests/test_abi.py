@@ -105,3 +105,15 @@ def test_python_api_rejects_cpu_tensors(satlib):
     x = torch.zeros(4, 4, dtype=torch.uint8)
     with pytest.raises(sat_gb300.SatError):
         sat_gb300.scanrow_brlt(x, torch.uint32)
+
+
+def test_cli_usage(satlib):
+    """The reference's command line (sat A S D0 D1 R) is built beside the
+    library; without arguments it prints its usage and exits 2."""
+    import subprocess
+    from sat_gb300 import build as B
+    r = subprocess.run([B.cli_path()], capture_output=True, text=True)
+    assert r.returncode == 2
+    assert "sat A S D0 D1 R" in r.stderr
+    r = subprocess.run([B.cli_path(), "3", "1", "0", "4", "1"], capture_output=True, text=True)
+    assert r.returncode == 2 and "not provided" in r.stderr

@@ -354,3 +354,20 @@ def test_full_size_4096_f64(cuda, oracle):
     a = oracle.gen("f64u", 4096, (4096, 4096))
     out = to_np(sat_gb300.sat(to_dev(a), torch.float64))
     _check_float(oracle, a, out, TOL[np.dtype(np.float64)])
+
+
+def test_cli_runs_reference_sizes(cuda):
+    """`sat 0 1 0 4 2`: u8 -> u32 ScanRow-BRLT at 1024^2 and 2048^2, one CSV
+    line per size in the reference's format."""
+    import subprocess
+    from sat_gb300 import build as B
+    r = subprocess.run([B.cli_path(), "0", "1", "0", "4", "2", "--reps", "3"], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().splitlines()
+    assert lines[0].startswith("uchar-->uint, ScanRow-BRLT, LF_SCAN")
+    for i, line in enumerate(lines[1:], start=1):
+        w, h, rest = line.split(", ", 2)
+        assert int(w) == int(h) == 1024 * i
+        assert rest.startswith("total time = ")
+        assert float(rest.split(", ")[-1]) > 0
