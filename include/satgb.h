@@ -139,6 +139,17 @@ typedef struct {
 
 satgb_status satgb_sat_ex(const satgb_sat_desc* desc, satgb_stream stream);
 
+/* Row-only and column-only scans, the two halves of ScanRowColumn as separate
+ * operations: out(y,x) = sum_{i<=x} in(y,i) (IncrementScanX::ScanX,
+ * integralImage/IncrementScanX.cu:12-113, and the first launch of
+ * ScanRowColumn.cu:475) and out(y,x) = sum_{j<=y} in(j,x) (IncrementScanY::ScanY,
+ * integralImage/IncrementScanY.cu:10-126).  Same type pairs, pitches and
+ * conventions as the SAT entry points. */
+satgb_status satgb_scan_rows(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch,
+                             void* d_out, int64_t out_pitch, int64_t width, int64_t height, satgb_stream stream);
+satgb_status satgb_scan_cols(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch,
+                             void* d_out, int64_t out_pitch, int64_t width, int64_t height, satgb_stream stream);
+
 /* The same SAT for a stack of n_planes equally sized images (e.g. the N*C
  * planes of an N x C x H x W tensor), plane p starting at d_in + p *
  * in_plane_stride and d_out + p * out_plane_stride (elements); each plane gets

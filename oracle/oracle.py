@@ -106,8 +106,9 @@ _I64 = ctypes.c_int64
 
 def _declare(L: ctypes.CDLL) -> None:
     for name in PAIRS:
-        for kind in ("serial", "reverse"):
-            f = getattr(L, f"oracle_sat_{kind}_{name}")
+        for fname in (f"oracle_sat_serial_{name}", f"oracle_sat_reverse_{name}", f"oracle_scan_rows_{name}",
+                      f"oracle_scan_cols_{name}"):
+            f = getattr(L, fname)
             f.argtypes = [_P, _I64, _P, _I64, _I64, _I64]
             f.restype = None
         f = getattr(L, f"oracle_sat_parallel_{name}")
@@ -160,6 +161,24 @@ def sat_parallel(a: np.ndarray, out_dtype, nthreads: int = 0) -> np.ndarray:
     out = np.empty((h, w), dtype=out_dtype)
     n = nthreads or lib().oracle_num_threads()
     getattr(lib(), f"oracle_sat_parallel_{name}")(_ptr(a), _pitch(a), _ptr(out), w, w, h, n)
+    return out
+
+
+def scan_rows(a: np.ndarray, out_dtype) -> np.ndarray:
+    """Row-only scan: IntegralRow (integralImage.h:74-82) on every row, as
+    IncrementScanX computes it; C restatement in the output type."""
+    h, w = a.shape
+    out = np.zeros((h, w), dtype=out_dtype)
+    getattr(lib(), f"oracle_scan_rows_{pair_name(a.dtype, out_dtype)}")(_ptr(a), _pitch(a), _ptr(out), w, w, h)
+    return out
+
+
+def scan_cols(a: np.ndarray, out_dtype) -> np.ndarray:
+    """Column-only scan: IntegralStride (integralImage.h:90-101) with the row
+    stride, on every column, as IncrementScanY computes it."""
+    h, w = a.shape
+    out = np.zeros((h, w), dtype=out_dtype)
+    getattr(lib(), f"oracle_scan_cols_{pair_name(a.dtype, out_dtype)}")(_ptr(a), _pitch(a), _ptr(out), w, w, h)
     return out
 
 

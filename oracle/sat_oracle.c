@@ -125,6 +125,35 @@ FOR_EACH_PAIR(DEF_SERIAL)
 FOR_EACH_PAIR(DEF_PARALLEL)
 
 /* ------------------------------------------------------------------ */
+/* Row-only and column-only scans: IntegralRow / IntegralStride        */
+/* (integralImage.h:74-101) applied to every row (stride 1) or every   */
+/* column (stride = pitch), as IncrementScanX/Y compute them.          */
+/* ------------------------------------------------------------------ */
+#define DEF_SCANS(NAME, TIN, TOUT, ACC, CVT)                                     \
+  void oracle_scan_rows_##NAME(const TIN* src, int64_t in_pitch, TOUT* dst,      \
+                               int64_t out_pitch, int64_t w, int64_t h) {        \
+    for (int64_t y = 0; y < h; ++y) {                                            \
+      ACC sum = 0;                                                               \
+      for (int64_t x = 0; x < w; ++x) {                                          \
+        sum += CVT(src[y * in_pitch + x]);                                       \
+        dst[y * out_pitch + x] = (TOUT)sum;                                      \
+      }                                                                          \
+    }                                                                            \
+  }                                                                              \
+  void oracle_scan_cols_##NAME(const TIN* src, int64_t in_pitch, TOUT* dst,      \
+                               int64_t out_pitch, int64_t w, int64_t h) {        \
+    for (int64_t x = 0; x < w; ++x) {                                            \
+      ACC sum = 0;                                                               \
+      for (int64_t y = 0; y < h; ++y) {                                          \
+        sum += CVT(src[y * in_pitch + x]);                                       \
+        dst[y * out_pitch + x] = (TOUT)sum;                                      \
+      }                                                                          \
+    }                                                                            \
+  }
+
+FOR_EACH_PAIR(DEF_SCANS)
+
+/* ------------------------------------------------------------------ */
 /* Reverse (suffix) SAT, the adjoint of the forward SAT:              */
 /*   R(y,x) = sum_{j>=y, i>=x} a(j,i),                                */
 /* computed in the same serial order mirrored (last row first, each   */

@@ -119,6 +119,27 @@ def scanrowcolumn(src: torch.Tensor, out_dtype=None, scan_type: int = LF_SCAN, o
     return _three("satgb_scanrowcolumn", src, out_dtype, scan_type, out, stream)
 
 
+def _scan(fn_name: str, src: torch.Tensor, out_dtype, out, stream) -> torch.Tensor:
+    _check_cuda(src)
+    out = _prep_out(src, out_dtype, out)
+    _check_cuda(out)
+    ip, ipitch, w, h = _image_args(src)
+    op, opitch, _, _ = _image_args(out)
+    check(getattr(_lib.load(), fn_name)(dtype_code(src.dtype), dtype_code(out.dtype), ip, ipitch, op, opitch, w, h,
+                                        _stream_handle(stream)))
+    return out
+
+
+def scan_rows(src: torch.Tensor, out_dtype=None, out=None, stream=None) -> torch.Tensor:
+    """Row-only scan, out(y,x) = sum_{i<=x} src(y,i) (IncrementScanX, IncrementScanX.cu:12-113)."""
+    return _scan("satgb_scan_rows", src, out_dtype, out, stream)
+
+
+def scan_cols(src: torch.Tensor, out_dtype=None, out=None, stream=None) -> torch.Tensor:
+    """Column-only scan, out(y,x) = sum_{j<=y} src(j,x) (IncrementScanY, IncrementScanY.cu:10-126)."""
+    return _scan("satgb_scan_cols", src, out_dtype, out, stream)
+
+
 ALGORITHMS = {
     "ScanRow-BRLT": scanrow_brlt,
     "BRLT-ScanRow": brlt_scanrow,

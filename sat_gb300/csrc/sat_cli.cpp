@@ -4,8 +4,8 @@
 //
 // mirrors `sat <algo> <scan> <dtIn> <dtOut> <repeat>` (pengdada/SAT
 // integralImage/main.cpp:8-44, GetArgs integralImage.h:56-63): A selects the
-// algorithm (0 ScanRow-BRLT, 1 BRLT-ScanRow, 2 ScanRowColumn; the column-only
-// and row-only tests 3 and 4 are not provided), S the warp scan (0
+// algorithm (0 ScanRow-BRLT, 1 BRLT-ScanRow, 2 ScanRowColumn, 3 the
+// column-only scan, 4 the row-only scan), S the warp scan (0
 // Kogge-Stone, 1 Ladner-Fischer), D0/D1 the input and output DataType codes
 // (integralImage.h:22-32), and R the sizes: square images of i*1024 for
 // i = 1..R, as the reference's drivers loop (ScanRow-BRLT.cu:272-273).
@@ -76,7 +76,7 @@ void fill01(std::vector<unsigned char>& buf, int t, size_t n, unsigned seed) {
 int usage() {
   std::fprintf(stderr,
                "usage: sat A S D0 D1 R [--reps N]\n"
-               "  A   0 ScanRow-BRLT, 1 BRLT-ScanRow, 2 ScanRowColumn\n"
+               "  A   0 ScanRow-BRLT, 1 BRLT-ScanRow, 2 ScanRowColumn, 3 column-only, 4 row-only\n"
                "  S   0 Kogge-Stone, 1 Ladner-Fischer\n"
                "  D0  input type, D1 output type: 0 u8, 1 i8, 4 u32, 5 i32, 6 f32, 7 f64\n"
                "  R   sizes i*1024 x i*1024 for i = 1..R\n");
@@ -101,15 +101,22 @@ int main(int argc, char** argv) {
   int reps = 1;
   for (int i = 6; i + 1 < argc; ++i)
     if (std::strcmp(argv[i], "--reps") == 0) reps = std::max(1, std::atoi(argv[i + 1]));
-  if (algo == 3 || algo == 4) {
-    std::fprintf(stderr, "the column-only / row-only scans (A = 3, 4) are not provided\n");
-    return 2;
-  }
-  if (algo < 0 || algo > 2 || repeat < 1 || type_size(d0) == 0 || type_size(d1) == 0) return usage();
+  if (algo < 0 || algo > 4 || repeat < 1 || type_size(d0) == 0 || type_size(d1) == 0) return usage();
   using Fn = satgb_status (*)(satgb_dtype, satgb_dtype, int, const void*, int64_t, void*, int64_t, int64_t,
                               int64_t, satgb_stream);
-  const Fn fns[3] = {&satgb_scanrow_brlt, &satgb_brlt_scanrow, &satgb_scanrowcolumn};
-  const char* names[3] = {"ScanRow-BRLT", "BRLT-ScanRow", "ScanRowColumn"};
+  // the single-direction scans take no scan type
+  struct Scans {
+    static satgb_status cols(satgb_dtype a, satgb_dtype b, int, const void* i, int64_t ip, void* o, int64_t op,
+                             int64_t w, int64_t h, satgb_stream s) {
+      return satgb_scan_cols(a, b, i, ip, o, op, w, h, s);
+    }
+    static satgb_status rows(satgb_dtype a, satgb_dtype b, int, const void* i, int64_t ip, void* o, int64_t op,
+                             int64_t w, int64_t h, satgb_stream s) {
+      return satgb_scan_rows(a, b, i, ip, o, op, w, h, s);
+    }
+  };
+  const Fn fns[5] = {&satgb_scanrow_brlt, &satgb_brlt_scanrow, &satgb_scanrowcolumn, &Scans::cols, &Scans::rows};
+  const char* names[5] = {"ScanRow-BRLT", "BRLT-ScanRow", "ScanRowColumn", "ScanY (column only)", "ScanX (row only)"};
   std::printf("%s-->%s, %s, %s\n", type_name(d0), type_name(d1), names[algo],
               scan == 0 ? "KoggeStone_SCAN" : "LF_SCAN");
   cudaStream_t stream;

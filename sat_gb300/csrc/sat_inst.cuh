@@ -11,7 +11,7 @@ namespace satgb {
 
 // Raises the kernel's dynamic shared-memory limit on the current device (once
 // per device); must precede occupancy queries and launches.
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
 cudaError_t prepare_impl() {
   using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   constexpr int kMaxDev = 64;
@@ -20,28 +20,28 @@ cudaError_t prepare_impl() {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
-  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB>,
+  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
   if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
   return e;
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
 cudaError_t launch_impl(const SatParams& p, int grid, cudaStream_t s) {
   using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
-  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB>();
+  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>();
   if (e != cudaSuccess) return e;
-  sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
   return cudaGetLastError();
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
 Variant make_variant(int in_t, int out_t, int mode, int cfg) {
   using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
-                 &launch_impl<TIn, TOut, A, REV, RPW, NW, MINB>,
-                 &prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB>,
-                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB>,
+                 &launch_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
+                 &prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
+                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
@@ -145,6 +145,14 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
       satgb::make_variant_r<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 3)
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
   SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
+
+// row-only and column-only scans (modes SG_MODE_ROWS / SG_MODE_COLS): the
+// pipelined 128-row tiles, forward
+#define SG_MODE_ROWS 2
+#define SG_MODE_COLS 3
+#define SG_SCANS(TIN, TOUT, A, IT, OT)                                                                       \
+  satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindRows>(IT, OT, SG_MODE_ROWS, 1), \
+      satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindCols>(IT, OT, SG_MODE_COLS, 1)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

@@ -622,7 +622,15 @@ __device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, 
 //
 // The reverse (suffix) SAT runs every scan in the opposite direction.
 // ---------------------------------------------------------------------------
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB>
+// What the tile kernel computes: the SAT, or only its row scan (each row's
+// prefix sums: the reference's ScanX, IncrementScanX.cu:12-113) or only its
+// column scan (ScanY, IncrementScanY.cu:10-126).  The single-direction scans
+// keep one look-back (rows or columns) and no corner.
+constexpr int kKindSat = 0;
+constexpr int kKindRows = 1;
+constexpr int kKindCols = 2;
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
 __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_constant__ SatParams P) {
   using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
   constexpr int CPT = SH::CPT;
@@ -799,7 +807,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       A ac = AR::zero();
 #pragma unroll
       for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colp[kk & 1][w][j]);
-      if ((REV ? (nxt.ty > 0) : (nxt.ty < nty - 1)) && !stall)
+      if (KIND != kKindRows && (REV ? (nxt.ty > 0) : (nxt.ty < nty - 1)) && !stall)
         publish<A>(P.col_words + ((unsigned long long)t * TW + j) * K, ac, tagA);
       A run = AR::zero();
 #pragma unroll
@@ -815,7 +823,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       lb_steps = REV ? (nty - 1 - nxt.ty) : nxt.ty;
     } else if (tid < TW + TH) {
       const int yy = tid - TW;
-      if ((REV ? (nxt.tx > 0) : (nxt.tx < ntx - 1)) && !stall)
+      if (KIND != kKindCols && (REV ? (nxt.tx > 0) : (nxt.tx < ntx - 1)) && !stall)
         publish<A>(P.row_words + ((unsigned long long)t * TH + yy) * K, s_rowagg[yy], tagA);
     } else if (warp == CW && lane == 0) {
       lb_base = P.corner_words + (unsigned long long)t * K;
@@ -842,14 +850,15 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       my_agg = agg_cur;
       // the current tile's first column / corner look-back window: read now,
       // used after A(k+1), so the round trip overlaps the local phase
-      if (tid < TW || (warp == CW && lane == 0)) early_read<A>(my_win, my_base, my_stride, my_steps);
+      if ((KIND != kKindRows && tid < TW) || (KIND == kKindSat && warp == CW && lane == 0))
+        early_read<A>(my_win, my_base, my_stride, my_steps);
     }
     // Row threads run the row look-back of the NEXT tile (k+1) in this
     // iteration, right after its local phase: its u (the corner aggregate)
     // then goes out without waiting for this CTA's corner of tile k.
     long long rt = -1;
     int rtx = 0, rty = 0, rntx = 1, rnty = 1;
-    if (tid >= TW && tid < TW + TH) {
+    if (KIND != kKindCols && tid >= TW && tid < TW + TH) {
       const int sn = (k + 1) % S; // tile k+1's stage: filled at least one iteration ago
       rt = s_tile[sn];
       if (rt >= 0) {
@@ -881,7 +890,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     // one look-back call site for the three roles (columns, rows, corner)
     A got = AR::zero();
     const bool lb_row = tid >= TW && tid < TW + TH && rt >= 0;
-    const bool lb_cur = has_cur && (tid < TW || (warp == CW && lane == 0));
+    const bool lb_cur =
+        has_cur && ((KIND != kKindRows && tid < TW) || (KIND == kKindSat && warp == CW && lane == 0));
     if (lb_row || lb_cur) {
       const long long stride = lb_row ? (REV ? 1 : -1) * (long long)TH * K : my_stride;
       const int steps = lb_row ? (REV ? (rntx - 1 - rtx) : rtx) : my_steps;
@@ -892,7 +902,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         // nothing to do for the columns before the first tile
       } else {
         const A above = got;
-        if (pub_col && !stall)
+        if (KIND != kKindRows && pub_col && !stall)
           publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
         s_colabove[tid] = above;
       }
@@ -927,7 +937,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
           for (int g = 0; g < TH / 32; ++g) u = AR::add(u, vload(&s_rlw[nb][g]));
           s_u[nb] = u;
-          if ((REV ? (rty > 0) : (rty < rnty - 1)) && !rstall)
+          if (KIND == kKindSat && (REV ? (rty > 0) : (rty < rnty - 1)) && !rstall)
             publish<A>(P.corner_words + (unsigned long long)rt * K, u, tagA);
         }
       }
@@ -936,7 +946,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       if (lane == 0 && has_cur) {
         // corner of tile k; its u was formed in the previous iteration
         s_corner = got;
-        if (pub_col && !stall)
+        if (KIND == kKindSat && pub_col && !stall)
           publish<A>(P.corner_words + (unsigned long long)t * K, AR::add(got, s_u[k & 1]), tagI);
       }
     } else if (tid == PT && producing && has_cur) {
@@ -992,6 +1002,11 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         const A base = AR::add(AR::add(corner, rl_prev), ex);
 #pragma unroll
         for (int c = 0; c < CPT; ++c) top[c] = AR::add(base, cp[c]);
+        if (KIND == kKindCols) {
+          // column scan: each column's carry only (no prefix over the columns)
+#pragma unroll
+          for (int c = 0; c < CPT; ++c) top[c] = AR::add(s_colabove[c * 32 + lane], s_colp[k & 1][warp][c * 32 + lane]);
+        }
       }
       TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
       TOut* so = reinterpret_cast<TOut*>(stages + st * STAGE_ELEMS) + (warp * RPW) * TW + lane * CPT;
@@ -1023,9 +1038,15 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
-          run = AR::add(run, Cvt<A, TIn>::in(x.u.e[c]));
-          top[c] = AR::add(top[c], run);
-          o.e[c] = OutCvt<TOut, A>::out(top[c]);
+          const A a = Cvt<A, TIn>::in(x.u.e[c]);
+          if (KIND == kKindCols) {
+            top[c] = AR::add(top[c], a);
+            o.e[c] = OutCvt<TOut, A>::out(top[c]);
+          } else {
+            run = AR::add(run, a);
+            if (KIND == kKindSat) top[c] = AR::add(top[c], run);
+            o.e[c] = OutCvt<TOut, A>::out(KIND == kKindRows ? run : top[c]);
+          }
         }
         *reinterpret_cast<uint4*>(so + r * TW) = o.v;
       }

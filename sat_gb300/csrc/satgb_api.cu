@@ -453,13 +453,18 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
   return SATGB_OK;
 }
 
+// internal modes of the variant table: the row-only and column-only scans
+constexpr int kModeRows = 2;
+constexpr int kModeCols = 3;
+
 satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in, long long in_pitch,
                         void* d_out, long long out_pitch, long long width, long long height,
                         cudaStream_t s, int force_cfg, long long planes = 1, long long in_plane = 0,
                         long long out_plane = 0) {
   const size_t in_sz = dtype_size(in_t), out_sz = dtype_size(out_t);
   if (!in_sz || !out_sz) return fail(SATGB_ERR_INVALID_ARG, "unknown dtype code (%d, %d)", in_t, out_t);
-  if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED) return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
+  if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED && mode != kModeRows && mode != kModeCols)
+    return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
   if (dir != SATGB_FORWARD && dir != SATGB_REVERSE) return fail(SATGB_ERR_INVALID_ARG, "unknown direction %d", dir);
   if (!pair_offered(in_t, out_t, mode))
     return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair %s -> %s%s not offered", dtype_name(in_t), dtype_name(out_t),
@@ -490,7 +495,8 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   st = get_device(&dev);
   if (st != SATGB_OK) return st;
   int cfg = force_cfg >= 0 ? force_cfg
-                           : choose_config_locked(in_t, out_t, mode, dir, width, height * std::max(1LL, planes), dev);
+            : (mode >= kModeRows) ? 1
+                                  : choose_config_locked(in_t, out_t, mode, dir, width, height * std::max(1LL, planes), dev);
   const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
@@ -594,8 +600,22 @@ satgb_status satgb_scanrowcolumn(satgb_dtype in_t, satgb_dtype out_t, int scan_t
                     height, (cudaStream_t)stream, -1);
 }
 
+satgb_status satgb_scan_rows(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch, void* d_out,
+                             int64_t out_pitch, int64_t width, int64_t height, satgb_stream stream) {
+  return sat_single(in_t, out_t, kModeRows, SATGB_FORWARD, d_in, in_pitch, d_out, out_pitch, width, height,
+                    (cudaStream_t)stream, -1);
+}
+
+satgb_status satgb_scan_cols(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch, void* d_out,
+                             int64_t out_pitch, int64_t width, int64_t height, satgb_stream stream) {
+  return sat_single(in_t, out_t, kModeCols, SATGB_FORWARD, d_in, in_pitch, d_out, out_pitch, width, height,
+                    (cudaStream_t)stream, -1);
+}
+
 satgb_status satgb_sat_ex(const satgb_sat_desc* d, satgb_stream stream) {
   if (!d) return fail(SATGB_ERR_INVALID_ARG, "null descriptor");
+  if (d->mode != SATGB_MODE_PLAIN && d->mode != SATGB_MODE_COMPENSATED)
+    return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", d->mode);
   return sat_single(d->in_t, d->out_t, d->mode, d->direction, d->d_in, d->in_pitch, d->d_out, d->out_pitch,
                     d->width, d->height, (cudaStream_t)stream, -1);
 }
@@ -603,6 +623,8 @@ satgb_status satgb_sat_ex(const satgb_sat_desc* d, satgb_stream stream) {
 satgb_status satgb_sat_planes(const satgb_sat_desc* d, int64_t n_planes, int64_t in_plane_stride,
                               int64_t out_plane_stride, satgb_stream stream) {
   if (!d) return fail(SATGB_ERR_INVALID_ARG, "null descriptor");
+  if (d->mode != SATGB_MODE_PLAIN && d->mode != SATGB_MODE_COMPENSATED)
+    return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", d->mode);
   return sat_single(d->in_t, d->out_t, d->mode, d->direction, d->d_in, d->in_pitch, d->d_out, d->out_pitch,
                     d->width, d->height, (cudaStream_t)stream, -1, n_planes, in_plane_stride, out_plane_stride);
 }
@@ -725,6 +747,7 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   const size_t in_sz = dtype_size(in_t), out_sz = dtype_size(out_t);
   if (!in_sz || !out_sz) return fail(SATGB_ERR_INVALID_ARG, "unknown dtype code");
   if (direction != SATGB_FORWARD && direction != SATGB_REVERSE) return fail(SATGB_ERR_INVALID_ARG, "unknown direction");
+  if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED) return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
   if (!pair_offered(in_t, out_t, mode)) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair not offered");
   if (n_images <= 0 || !images) return fail(SATGB_ERR_INVALID_ARG, "empty image list");
   cudaStream_t s = (cudaStream_t)stream;

@@ -84,6 +84,8 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
   if (!in_sz || !out_sz) return noalloc_fail(SATGB_ERR_UNSUPPORTED_TYPES, "dtype pair not offered");
   if (d->direction != SATGB_FORWARD && d->direction != SATGB_REVERSE)
     return noalloc_fail(SATGB_ERR_INVALID_ARG, "unknown direction");
+  if (d->mode != SATGB_MODE_PLAIN && d->mode != SATGB_MODE_COMPENSATED)
+    return noalloc_fail(SATGB_ERR_INVALID_ARG, "unknown mode");
   const Variant* v = find_variant(d->in_t, d->out_t, d->mode, d->direction, kNoallocConfig);
   if (!v) return noalloc_fail(SATGB_ERR_UNSUPPORTED_TYPES, "dtype pair / mode not offered");
   if (d->width < 0 || d->height < 0) return noalloc_fail(SATGB_ERR_INVALID_ARG, "negative width/height");

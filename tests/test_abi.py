@@ -115,5 +115,5 @@ def test_cli_usage(satlib):
     r = subprocess.run([B.cli_path()], capture_output=True, text=True)
     assert r.returncode == 2
     assert "sat A S D0 D1 R" in r.stderr
-    r = subprocess.run([B.cli_path(), "3", "1", "0", "4", "1"], capture_output=True, text=True)
-    assert r.returncode == 2 and "not provided" in r.stderr
+    r = subprocess.run([B.cli_path(), "5", "1", "0", "4", "1"], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr

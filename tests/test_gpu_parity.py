@@ -371,3 +371,48 @@ def test_cli_runs_reference_sizes(cuda):
         assert int(w) == int(h) == 1024 * i
         assert rest.startswith("total time = ")
         assert float(rest.split(", ")[-1]) > 0
+
+
+SCAN_TORCH = {np.dtype(np.uint32): torch.uint32, np.dtype(np.int32): torch.int32,
+              np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64}
+
+
+@pytest.mark.parametrize("which", ["rows", "cols"])
+def test_row_and_column_scans_all_pairs(cuda, oracle, which):
+    """satgb_scan_rows / satgb_scan_cols (ScanX / ScanY as separate ops) against
+    IntegralRow / IntegralStride: bit-exact for integer outputs; floats within
+    1e-5 (f32) / 1e-13 (f64) of the FP64 scan, relative to the scan of |a|."""
+    fn = sat_gb300.scan_rows if which == "rows" else sat_gb300.scan_cols
+    ref = oracle.scan_rows if which == "rows" else oracle.scan_cols
+    axis = 1 if which == "rows" else 0
+    for name, (ti, to) in oracle.PAIRS.items():
+        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (129, 257), (517, 769)]):
+            a = oracle.gen(PAIR_KINDS[ti], 3000 + i, shape)
+            out = to_np(fn(to_dev(a), SCAN_TORCH[np.dtype(to)]))
+            if np.dtype(to).kind in "iu":
+                assert np.array_equal(bits(out), bits(ref(a, to))), (which, name, shape)
+            else:
+                exact = np.cumsum(a.astype(np.float64), axis=axis)
+                den = np.cumsum(np.abs(a.astype(np.float64)), axis=axis)
+                err = np.abs(out.astype(np.float64) - exact) / np.maximum(den, 1e-300)
+                assert err.max() <= TOL[np.dtype(to)], (which, name, shape, err.max())
+
+
+def test_scans_pitched_and_full_size(cuda, oracle):
+    """Pitched u8 -> u32 rows and columns, and an 8192 x 8192 check of
+    sum(row scan) == sum(column scan) == the SAT's last element, mod 2^32."""
+    a = oracle.gen("u8", 91, (333, 555))
+    src = empty_pitched(333, 555, 640, torch.uint8)
+    src.copy_(to_dev(a))
+    for fn, ref in ((sat_gb300.scan_rows, oracle.scan_rows), (sat_gb300.scan_cols, oracle.scan_cols)):
+        dst = empty_pitched(333, 555, 600, torch.uint32, fill=-1)
+        fn(src, torch.uint32, out=dst)
+        assert np.array_equal(to_np(dst), ref(a, np.uint32))
+    x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda)
+    r = sat_gb300.scan_rows(x, torch.uint32)
+    c = sat_gb300.scan_cols(x, torch.uint32)
+    s = sat_gb300.sat(x, torch.uint32)
+    total = int(x.to(torch.int64).sum().item()) % (1 << 32)
+    assert int(r[:, -1].view(torch.int32).to(torch.int64).remainder(1 << 32).sum().item()) % (1 << 32) == total
+    assert int(c[-1, :].view(torch.int32).to(torch.int64).remainder(1 << 32).sum().item()) % (1 << 32) == total
+    assert int(s[-1, -1].view(torch.int32).to(torch.int64).item()) % (1 << 32) == total

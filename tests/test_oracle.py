@@ -129,3 +129,16 @@ def test_reference_live_matches_port(oracle):
     for t, kind in [(np.uint32, "u32"), (np.int32, "i32"), (np.float32, "f32u"), (np.float64, "f64u")]:
         a = oracle.gen(kind, 22, (77, 91))
         assert np.array_equal(_bits(oracle.ref_parallel(a)), _bits(oracle.sat_parallel(a, t)))
+
+
+def test_oracle_row_and_column_scans(oracle):
+    """IntegralRow / IntegralStride restated (integralImage.h:74-101): integer
+    pairs equal numpy's cumsum in the output type (wrapping mod 2^32)."""
+    for name in ("u8_u32", "i8_i32", "i32_i32", "u32_u32"):
+        ti, to = oracle.PAIRS[name]
+        kind = {np.uint8: "u8", np.int8: "i8", np.int32: "i32", np.uint32: "u32"}[ti]
+        a = oracle.gen(kind, 77, (41, 67)).astype(ti)
+        acc = a.astype(np.int64).astype(np.uint32)
+        with np.errstate(over="ignore"):
+            assert np.array_equal(oracle.scan_rows(a, to).view(np.uint32), np.cumsum(acc, axis=1, dtype=np.uint32))
+            assert np.array_equal(oracle.scan_cols(a, to).view(np.uint32), np.cumsum(acc, axis=0, dtype=np.uint32))
