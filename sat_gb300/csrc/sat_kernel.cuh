@@ -525,7 +525,15 @@ struct TilePlan {
 };
 
 // Maps ticket `tk` to its tile.
-template <bool REV>
+// Tile orders inside a plane: anti-diagonal for the SAT (both neighbours
+// precede a tile by about a diagonal); row-major when tiles depend only on the
+// tile above (column scan), column-major when only on the tile to the left
+// (row scan) -- the orders whose concurrent tiles lie closest in memory.
+constexpr int kOrderDiag = 0;
+constexpr int kOrderRows = 1;
+constexpr int kOrderCols = 2;
+
+template <bool REV, int ORDER = kOrderDiag>
 __device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long long tk) {
   TilePlan tp;
   tp.t = -1;
@@ -548,7 +556,16 @@ __device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long lon
   const long long local = q - D->tile_base;
   const long long pl = local / D->tiles_per_plane;
   int tx, ty;
-  diag_tile(local - pl * D->tiles_per_plane, ntx, nty, tx, ty);
+  const long long li = local - pl * D->tiles_per_plane;
+  if (ORDER == kOrderRows) {
+    ty = (int)(li / ntx);
+    tx = (int)(li - (long long)ty * ntx);
+  } else if (ORDER == kOrderCols) {
+    tx = (int)(li / nty);
+    ty = (int)(li - (long long)tx * nty);
+  } else {
+    diag_tile(li, ntx, nty, tx, ty);
+  }
   tp.t = D->tile_base + pl * D->tiles_per_plane + (long long)ty * ntx + tx;
   tp.tx = tx;
   tp.ty = ty;
@@ -586,11 +603,11 @@ __device__ __forceinline__ void issue_tile(const SatParams& P, const TilePlan& t
 // Takes ticket `tk`, maps it to a tile and starts its input on its way into
 // stage `st`.  Returns false once the tickets are exhausted (the stage then
 // carries -1).
-template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES>
+template <class TIn, bool REV, int TW, int TH, int STAGE_BYTES, int ORDER = kOrderDiag>
 __device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, int st, TIn* stage_ptr,
                                         long long* s_tile, int* s_img, int* s_tx, int* s_ty, int* s_pl,
                                         unsigned long long* s_full) {
-  const TilePlan tp = plan_tile<REV>(P, tk);
+  const TilePlan tp = plan_tile<REV, ORDER>(P, tk);
   issue_tile<TIn, TW, TH, STAGE_BYTES>(P, tp, st, stage_ptr, s_tile, s_img, s_tx, s_ty, s_pl, s_full);
   return tp.t >= 0;
 }
@@ -652,6 +669,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   constexpr int CH = RP;             // ... and values per lane
   constexpr int K = Ar<A>::K;
   constexpr bool WIDEN = sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
+  constexpr int ORDER = KIND == kKindCols ? kOrderRows : KIND == kKindRows ? kOrderCols : kOrderDiag;
   using AR = Ar<A>;
 
   extern __shared__ __align__(128) unsigned char dsmem[];
@@ -692,7 +710,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 #pragma unroll
     for (int s = 0; s < S - 1; ++s) {
       if (producing)
-        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, atomicAdd(&P.ws->ticket, 1ull), s,
+        producing = produce<TIn, REV, TW, TH, SH::IN_BYTES, ORDER>(P, atomicAdd(&P.ws->ticket, 1ull), s,
                                                             stages + s * STAGE_ELEMS, s_tile, s_img, s_tx, s_ty,
                                                             s_pl, s_full);
     }
@@ -758,9 +776,9 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       rowp[r] = rs;
     }
     // row partials -> exclusive prefix over the lanes (E) and the row totals,
-    // RP rows per pass through the transpose scratch
+    // RP rows per pass through the transpose scratch (not for the column scan)
 #pragma unroll
-    for (int h = 0; h < RPW / RP; ++h) {
+    for (int h = 0; h < (KIND == kKindCols ? 0 : RPW / RP); ++h) {
 #pragma unroll
       for (int r = 0; r < RP; ++r) s_tr[warp][r][lane ^ r] = rowp[h * RP + r];
       __syncwarp();
@@ -953,7 +971,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       // tile k+S-1 into the stage whose store (tile k-1) has finished reading it
       const int ps = (st + S - 1) % S;
       bulk_wait_read_all();
-      producing = produce<TIn, REV, TW, TH, SH::IN_BYTES>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile, s_img,
+      producing = produce<TIn, REV, TW, TH, SH::IN_BYTES, ORDER>(P, pending, ps, stages + ps * STAGE_ELEMS, s_tile, s_img,
                                                           s_tx, s_ty, s_pl, s_full);
       if (producing) pending = atomicAdd(&P.ws->ticket, 1ull);
     }
