@@ -76,6 +76,24 @@ def test_planes_pitched_and_reverse(cuda, oracle):
         assert np.max(np.abs(outf[i] - ref) / np.maximum(den, 1e-30)) <= 1e-5
 
 
+@pytest.mark.parametrize("mode", ["plain", "compensated"])
+def test_planes_float_modes(cuda, oracle, mode):
+    """Stacks through the default kernels of each accumulator: f64 outputs
+    (warp-specialized tiles) and compensated f32 (register tiles)."""
+    p, h, w = 6, 77, 301
+    a = oracle.gen("f32n", 15, (p * h, w)).astype(np.float32).reshape(p, h, w)
+    if mode == "plain":
+        out = to_np(sat_gb300.sat(to_dev(a), torch.float64))
+        tol = 1e-13
+    else:
+        out = to_np(sat_gb300.sat(to_dev(a), torch.float32, mode="compensated"))
+        tol = 2e-7
+    for i in range(p):
+        ref = oracle.sat_fp64(a[i])
+        den = oracle.sat_fp64(a[i], absval=True)
+        assert np.max(np.abs(out[i].astype(np.float64) - ref) / np.maximum(den, 1e-30)) <= tol, i
+
+
 def test_planes_many_small(cuda, oracle):
     """More planes than tiles per plane: 300 planes of 40 x 70."""
     a = oracle.gen("u8", 14, (300 * 40, 70)).reshape(300, 40, 70)
