@@ -298,7 +298,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: torch.rand uniform [0,1) f32 (seeded); inputs and outputs 256 MiB each, larger than L2, no flush",
-        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step (BASELINE configs[1])",
+        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step",
                    "width": W_HEAD, "height": H_HEAD, "in_dtype": "f32", "out_dtype": "f32",
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas{world}"},
         "e2e": e2e,
@@ -364,7 +364,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: splitmix64 uniform [0,1) f32 (seeded)",
-        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step (BASELINE configs[1])",
+        "config": {"workload": "f32->f32 plain SAT, one 8192x8192 image per step",
                    "width": W_HEAD, "height": H_HEAD, "in_dtype": "f32", "out_dtype": "f32"},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": n, "kind": "port",
                          "sample": f"each step one full 8192x8192 f32 IntegralImageParallel (oracle restatement), {n} OpenMP threads"},

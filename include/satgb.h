@@ -24,7 +24,7 @@
  *   - scan_type is the reference's SCAN enum (integralImage.h:34-37).
  *     Kogge-Stone and Ladner-Fischer give identical integer results; for
  *     floating point this library's summation tree is its own and floats are
- *     judged against an FP64 oracle, so scan_type is validated and recorded
+ *     checked against an FP64 oracle, so scan_type is validated and recorded
  *     but does not change the arithmetic.
  * Added over the reference (which reports no errors: CUDA_CHECK_ERROR is an
  * empty macro, cudaLib.cuh:21-22): every call returns a satgb_status; calls

@@ -1,8 +1,8 @@
 """Multi-plane SATs, box filters and their autograd backward on the GPU.
 
 Plane stacks are integer-exact against the oracle plane by plane.  Box means
-and gradients are floating point (f32 through an f32 SAT) and are judged
-against float64 torch references with the tolerances written below:
+and gradients are floating point (f32 through an f32 SAT) and are compared
+with float64 torch references with the tolerances written below:
 
   box means        |m - m64| <= 4 * eps32 * max|S64| / area + 1e-7
   gradients        |g - g64| <= 1e-4 * max(1, max|g64|)

@@ -2,7 +2,7 @@
 
 Integer outputs must be bit-exact against the reference's CPU integral image
 (golden vectors made by running it, and the C restatement for other inputs),
-including the mod-2^32 wrap.  Float outputs are judged against the FP64
+including the mod-2^32 wrap.  Float outputs are compared with the FP64
 oracle with the tolerances below, stated relative to SAT(|a|) computed in
 FP64 (the denominator that stays meaningful under cancellation):
 
