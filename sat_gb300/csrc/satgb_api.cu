@@ -276,6 +276,21 @@ satgb_status ensure_ws(Workspace& ws, size_t bytes, cudaStream_t s) {
 struct DevInfo {
   int sms = 0;
 };
+
+// descriptor cache of sat_single (guarded by g_mu)
+struct DescKey {
+  const Variant* v;
+  int in_t, out_t;
+  const void* in;
+  const void* out;
+  long long in_pitch, out_pitch, width, height, planes, in_plane, out_plane;
+  bool operator<(const DescKey& o) const {
+    return std::tie(v, in_t, out_t, in, out, in_pitch, out_pitch, width, height, planes, in_plane, out_plane) <
+           std::tie(o.v, o.in_t, o.out_t, o.in, o.out, o.in_pitch, o.out_pitch, o.width, o.height, o.planes,
+                    o.in_plane, o.out_plane);
+  }
+};
+std::map<DescKey, ImageDesc> g_desc_cache;
 std::map<int, DevInfo> g_dev;
 std::map<std::pair<int, const void*>, int> g_occ; // (device, kernel) -> CTAs per SM
 
@@ -501,7 +516,22 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
   ImageDesc d;
-  fill_image_desc(d, v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, 0, planes, in_plane, out_plane);
+  {
+    // Encoding the two tensor maps costs host time comparable to a small
+    // image's kernel; repeated calls on the same buffers (benchmarks, serving
+    // loops) reuse the descriptor.  A map holds the buffer's address, so the key
+    // is every argument of fill_image_desc.
+    const DescKey key{v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, planes, in_plane, out_plane};
+    auto it = g_desc_cache.find(key);
+    if (it != g_desc_cache.end()) {
+      d = it->second;
+    } else {
+      fill_image_desc(d, v, in_t, out_t, d_in, d_out, in_pitch, out_pitch, width, height, 0, planes, in_plane,
+                      out_plane);
+      if (g_desc_cache.size() >= 64) g_desc_cache.clear();
+      g_desc_cache.emplace(key, d);
+    }
+  }
   const long long n_tiles = (long long)d.ntx * d.nty * d.planes;
   if ((long long)d.ntx * v->TW < width || n_tiles > (1LL << 40))
     return fail(SATGB_ERR_OVERFLOW, "image too large (%lld x %lld)", width, height);
@@ -683,6 +713,7 @@ satgb_status satgb_release(void) {
   cudaDeviceSynchronize();
   for (auto& kv : g_ws) ws_free(kv.second.base);
   g_ws.clear();
+  g_desc_cache.clear();
   return SATGB_OK;
 }
 
