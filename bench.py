@@ -116,6 +116,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": n}
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """The slowest rank's time (replicas: every rank processes its own image)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, steps: int, step_bytes: int, total_ms: float) -> float:
+    """Whole-job GB/s: every rank's steps over the slowest rank's time."""
+    return world * steps * step_bytes / (total_ms / 1e3) / GB
+
+
 def _time_steps(fn, steps, warmup, stream, min_warm_s=1.0):
     """W untimed warm-up steps (at least min_warm_s of work, so the clock
     sampler sees the GPU under load), then exactly `steps` timed steps with
@@ -184,14 +198,12 @@ def run_gpu(args):
     launches = sat_gb300.launch_count() - l0
     sat_gb300.stream_check()
     if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dev)
         torch.distributed.barrier()
     clocks = sampler.stop() if rank == 0 else None
     timed_launches = args.steps  # one launch per step
     warm_launches = launches - timed_launches
-    value = world * args.steps * step_bytes / (total_ms / 1e3) / GB
+    value = replica_throughput(world, args.steps, step_bytes, total_ms)
     avg_launch_ms = statistics.mean(per)
     achieved = step_bytes / (avg_launch_ms / 1e3) / GB
 
