@@ -318,36 +318,6 @@ static __device__ __noinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t par
   }
 }
 
-// Spins until the K-word status value at `w` is valid for this launch.
-// The wait is bounded: after wait_limit_ns (or when another wait of this
-// launch already failed) it records SATGB_ERR_TIMEOUT in the workspace
-// header, returns a zero "inclusive" value and lets the kernel run to its end,
-// so the context stays usable and the host reports the error.
-template <class A>
-__device__ __noinline__ uint32_t wait_read(const unsigned long long* w, uint32_t tag_agg,
-                                           uint32_t tag_inc, A& val, const SatParams& P,
-                                           long long tile) {
-  uint32_t st = try_read<A>(w, tag_agg, tag_inc, val);
-  if (st) return st;
-  const unsigned long long t0 = global_timer_ns();
-  unsigned ns = 20;
-  for (uint32_t it = 0;; ++it) {
-    __nanosleep(ns);
-    if (ns < 256) ns <<= 1;
-    st = try_read<A>(w, tag_agg, tag_inc, val);
-    if (st) return st;
-    if ((it & 15u) == 15u) {
-      bool give_up = ld_relaxed_u32(&P.ws->error) != 0u ||
-                     (long long)(global_timer_ns() - t0) > P.wait_limit_ns || it > (1u << 26);
-      if (give_up) {
-        record_error(P, tile);
-        val = Ar<A>::zero();
-        return kStateInc;
-      }
-    }
-  }
-}
-
 // Ticket -> tile.  Tiles of one image are ordered by anti-diagonal d = tx+ty,
 // then by ty; P(d) = number of tiles on diagonals < d.
 __device__ __forceinline__ long long diag_prefix(long long d, long long ntx, long long nty) {

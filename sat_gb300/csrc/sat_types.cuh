@@ -207,24 +207,4 @@ static_assert(sizeof(WsHeader) == 64, "header is one 64-byte block");
 
 constexpr uint32_t kDevErrTimeout = 7u; // == SATGB_ERR_TIMEOUT
 
-// Reads a K-word status value; returns 0 = not ready, else its state.
-template <class A>
-__device__ __forceinline__ uint32_t try_read(const unsigned long long* words, uint32_t tag_agg,
-                                             uint32_t tag_inc, A& val) {
-  constexpr int K = Ar<A>::K;
-  uint32_t p[K];
-  uint32_t tag0 = 0;
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    unsigned long long w = ld_relaxed_u64(words + k);
-    uint32_t tag = (uint32_t)(w >> 32);
-    if (k == 0) tag0 = tag;
-    else if (tag != tag0) return 0u;
-    p[k] = (uint32_t)w;
-  }
-  if (tag0 != tag_agg && tag0 != tag_inc) return 0u;
-  val = Ar<A>::from_words(p);
-  return tag0 & 3u;
-}
-
 }  // namespace satgb
