@@ -274,16 +274,18 @@ def test_batch_plan_float_and_reverse(cuda, oracle):
         plan.close()
 
 
-def test_timeout_is_reported_and_context_survives(cuda, oracle):
-    """A tile that never publishes makes its dependents hit the wait limit;
-    the call reports SATGB_ERR_TIMEOUT and the next call is correct."""
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+def test_timeout_is_reported_and_context_survives(cuda, oracle, cfg):
+    """A tile that never publishes makes its dependents hit the wait limit
+    (every kernel: warp-specialized, pipelined, register-resident); the call
+    reports SATGB_ERR_TIMEOUT and the next call is correct."""
     L = _lib.load()
     a = oracle.gen("u8", 77, (512, 512))
     x = to_dev(a)
     s = torch.cuda.Stream()
     try:
         sat_gb300.set_wait_limit_us(20_000)
-        sat_gb300.set_config(0)
+        sat_gb300.set_config(cfg)
         assert L.satgb_debug_stall_tile(5) == 0
         with torch.cuda.stream(s):
             sat_gb300.scanrow_brlt(x, torch.uint32)
