@@ -34,6 +34,7 @@ struct BoxArgs {
   float* sat;
   int64_t sat_pitch, sat_plane;
   int nr;
+  int rmax; // the largest radius
   int r[SATGB_MAX_RADII];
   float inv_full[SATGB_MAX_RADII]; // 1 / (2r + 1): the reciprocal window length away from the edges
   float* box[SATGB_MAX_RADII];
@@ -43,6 +44,9 @@ struct BoxArgs {
 // A block covers 32 columns x 64 rows of one plane: blockDim (32, 8), each
 // thread 8 rows 8 apart, so a warp touches 32 consecutive columns of a row.
 constexpr int kBX = 32, kBY = 8, kRows = 8;
+// The backward blocks are 32 rows tall (4 rows a thread): the blocks that
+// touch the 2r-wide border band, which take the general path, are fewer.
+constexpr int kBRows = 4;
 
 // Window [lo, hi] of radius r around i, clipped to [0, n-1], and 1 / its length.
 struct Win {
@@ -56,11 +60,21 @@ __device__ __forceinline__ Win win(int i, int r, int n, float inv_full) {
   if (i - r >= 0 && i + r <= n - 1) {
     w.inv = inv_full; // the whole window fits: the common case, no division
   } else {
-    w.inv = 1.0f / (float)(w.hi - w.lo + 1);
+    w.inv = __frcp_rn((float)(w.hi - w.lo + 1)); // the correctly rounded 1/len, as 1.0f / len
   }
   return w;
 }
 
+// A block is interior for the forward pass when every output in it has its
+// whole window and the row and column before it inside the image, for the
+// largest radius and so for all: then the four corners sit at fixed offsets and
+// a thread issues all its rows' corner loads before it needs them.
+__device__ __forceinline__ bool fwd_block_interior(const BoxArgs& a, int x0, int y0) {
+  const int W = (int)a.w, H = (int)a.h, r = a.rmax;
+  return x0 - r - 1 >= 0 && x0 + kBX - 1 + r <= W - 1 && y0 - r - 1 >= 0 && y0 + kBY * kRows - 1 + r <= H - 1;
+}
+
+template <int NR>
 __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constant__ BoxArgs a) {
   const int W = (int)a.w, H = (int)a.h;
   const int x = blockIdx.x * kBX + threadIdx.x;
@@ -68,8 +82,28 @@ __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constan
   const long long pl = blockIdx.z;
   const float* S = a.sat + pl * a.sat_plane;
   const int ybase = blockIdx.y * (kBY * kRows) + threadIdx.y;
+  if (fwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kRows))) {
+    const long long sp = a.sat_pitch, bp = a.box_pitch;
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+      const int r = a.r[i];
+      const float inv2 = a.inv_full[i] * a.inv_full[i];
+      const float* hi = S + (long long)(ybase + r) * sp + x;
+      const float* lo = hi - (long long)(2 * r + 1) * sp;
+      float* B = a.box[i] + pl * a.box_plane + (long long)ybase * bp + x;
+      float out[kRows];
+#pragma unroll
+      for (int k = 0; k < kRows; ++k) {
+        const long long o = (long long)k * kBY * sp;
+        out[k] = ((__ldg(hi + o + r) - __ldg(hi + o - r - 1)) - (__ldg(lo + o + r) - __ldg(lo + o - r - 1))) * inv2;
+      }
+#pragma unroll
+      for (int k = 0; k < kRows; ++k) __stcs(B + (long long)k * kBY * bp, out[k]);
+    }
+    return;
+  }
 #pragma unroll 1
-  for (int i = 0; i < a.nr; ++i) {
+  for (int i = 0; i < NR; ++i) {
     const int r = a.r[i];
     const float inv_full = a.inv_full[i];
     const float inv2 = inv_full * inv_full;
@@ -145,68 +179,146 @@ __device__ __noinline__ float adjoint_edge(const float* g, long long pitch, int 
   return t;
 }
 
-__global__ void __launch_bounds__(kBX * kBY, 4) box_bwd_kernel(const __grid_constant__ BoxArgs a) {
+// adjoint_edge for one element, summed by the 32 lanes of a warp together:
+// lane l takes taps l, l + 32, ... of the (rows x columns) tap set, and a
+// butterfly sum gives every lane the same total.  Used for the corner
+// (H-1, W-1), whose (r + 1)^2 taps would otherwise fall to a single lane.
+__device__ __noinline__ float adjoint_edge_warp(const float* g, long long pitch, int pr, int q, int r, int H, int W,
+                                                int lane) {
+  const int ylo = pr < H - 1 ? pr - r : max(0, H - 1 - r);
+  const int yhi = pr < H - 1 ? pr - r : H - 1;
+  const int xlo = q < W - 1 ? q - r : max(0, W - 1 - r);
+  const int xhi = q < W - 1 ? q - r : W - 1;
+  const int y2 = pr + 1 + r, x2 = q + 1 + r;
+  const int y0 = max(0, ylo), x0 = max(0, xlo);
+  const int npy = yhi >= y0 ? yhi - y0 + 1 : 0, npx = xhi >= x0 ? xhi - x0 + 1 : 0;
+  const int ny = npy + (y2 <= H - 1 ? 1 : 0), nx = npx + (x2 <= W - 1 ? 1 : 0);
+  float s = 0.f;
+  for (int t = lane; t < ny * nx; t += 32) {
+    const int iy = t / nx, ix = t - iy * nx;
+    const int y = iy < npy ? y0 + iy : y2;
+    const int x = ix < npx ? x0 + ix : x2;
+    const float v = h_at(g, pitch, y, x, r, H, W);
+    s += (iy < npy) == (ix < npx) ? v : -v;
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  return s;
+}
+
+// A block is interior for the backward pass when the four outputs with a
+// corner at each of its positions have whole windows, for every radius: then
+// the taps sit at fixed offsets (and the block misses the last row and column).
+__device__ __forceinline__ bool bwd_block_interior(const BoxArgs& a, int x0, int y0) {
+  const int W = (int)a.w, H = (int)a.h, r2 = 2 * a.rmax;
+  return x0 >= r2 && x0 + kBX - 1 <= W - 2 - r2 && y0 >= r2 && y0 + kBY * kBRows - 1 <= H - 2 - r2;
+}
+
+template <int NR>
+__global__ void __launch_bounds__(kBX * kBY, 3) box_bwd_kernel(const __grid_constant__ BoxArgs a) {
   const int W = (int)a.w, H = (int)a.h;
   const int q = blockIdx.x * kBX + threadIdx.x;
-  if (q >= W) return;
   const long long pl = blockIdx.z;
-  const int ybase = blockIdx.y * (kBY * kRows) + threadIdx.y;
-  const bool col_edge = q == W - 1;
+  const int ybase = blockIdx.y * (kBY * kBRows) + threadIdx.y;
+  if (bwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kBRows))) {
+    // dS(p,q) = sum_i c_i ((g(p-r,q-r) - g(p-r,q+1+r)) - (g(p+1+r,q-r) - g(p+1+r,q+1+r)))
+    const long long gp = a.box_pitch;
+    float acc[kBRows];
+#pragma unroll
+    for (int k = 0; k < kBRows; ++k) acc[k] = 0.f;
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+      const int r = a.r[i];
+      const int d = 2 * r + 1;
+      const float c = a.inv_full[i] * a.inv_full[i];
+      const float* t = a.box[i] + pl * a.box_plane + (long long)(ybase - r) * gp + (q - r);
+      const float* b = t + (long long)d * gp;
+#pragma unroll
+      for (int k = 0; k < kBRows; ++k) {
+        const long long o = (long long)k * kBY * gp;
+        acc[k] += ((__ldg(t + o) - __ldg(t + o + d)) - (__ldg(b + o) - __ldg(b + o + d))) * c;
+      }
+    }
+    float* dS = a.sat + pl * a.sat_plane + (long long)ybase * a.sat_pitch + q;
+#pragma unroll
+    for (int k = 0; k < kBRows; ++k) __stcs(dS + (long long)k * kBY * a.sat_pitch, acc[k]);
+    return;
+  }
+  const bool live = q < W;
   // per radius: +h at column q - r, -h at column q + 1 + r (when inside),
   // each with its reciprocal window width (0 marks a column outside)
-  float ixp[SATGB_MAX_RADII], ixm[SATGB_MAX_RADII];
+  float ixp[NR], ixm[NR];
 #pragma unroll
-  for (int i = 0; i < SATGB_MAX_RADII; ++i) {
-    ixp[i] = ixm[i] = 0.f;
-    if (i < a.nr) {
-      const int r = a.r[i];
-      if (q - r >= 0) ixp[i] = win(q - r, r, W, a.inv_full[i]).inv;
-      if (q + 1 + r <= W - 1) ixm[i] = win(q + 1 + r, r, W, a.inv_full[i]).inv;
+  for (int i = 0; i < NR; ++i) {
+    const int r = a.r[i];
+    ixp[i] = live && q - r >= 0 ? win(q - r, r, W, a.inv_full[i]).inv : 0.f;
+    ixm[i] = live && q + 1 + r <= W - 1 ? win(q + 1 + r, r, W, a.inv_full[i]).inv : 0.f;
+  }
+  // Every row at once and without branches: a tap outside the image reads
+  // nothing and counts 0; 1/(window length) of a tap row is inv_full unless the
+  // window is clipped.  The last row and column are summed apart below.
+  const long long gp = a.box_pitch;
+  float acc[kBRows];
+#pragma unroll
+  for (int k = 0; k < kBRows; ++k) acc[k] = 0.f;
+#pragma unroll
+  for (int i = 0; i < NR; ++i) {
+    const int r = a.r[i];
+    const float* g = a.box[i] + pl * a.box_plane;
+    const int xp = q - r, xm = q + 1 + r;
+    const bool okp = live && xp >= 0, okm = live && xm <= W - 1;
+#pragma unroll
+    for (int k = 0; k < kBRows; ++k) {
+      const int pr = ybase + k * kBY;
+      const int yp = pr - r, ym = pr + 1 + r;
+      const bool oyp = yp >= 0 && pr < H, oym = ym <= H - 1;
+      const float iyp = !oyp ? 0.f : (yp >= r && yp + r <= H - 1 ? a.inv_full[i] : win(yp, r, H, a.inv_full[i]).inv);
+      const float iym = !oym ? 0.f : (ym >= r && ym + r <= H - 1 ? a.inv_full[i] : win(ym, r, H, a.inv_full[i]).inv);
+      const float* rp = g + (long long)yp * gp;
+      const float* rm = g + (long long)ym * gp;
+      const float a0 = oyp && okp ? __ldg(rp + xp) : 0.f;
+      const float a1 = oyp && okm ? __ldg(rp + xm) : 0.f;
+      const float b0 = oym && okp ? __ldg(rm + xp) : 0.f;
+      const float b1 = oym && okm ? __ldg(rm + xm) : 0.f;
+      acc[k] += (a0 * ixp[i] - a1 * ixm[i]) * iyp - (b0 * ixp[i] - b1 * ixm[i]) * iym;
     }
   }
+  // the last row and column belong to box_bwd_edge_kernel
   float* dS = a.sat + pl * a.sat_plane;
-#pragma unroll 2
-  for (int k = 0; k < kRows; ++k) {
-    const int pr = ybase + k * kBY;
-    if (pr >= H) break;
-    float acc = 0.f;
-    if (col_edge || pr == H - 1) {
-      for (int i = 0; i < a.nr; ++i)
-        acc += adjoint_edge(a.box[i] + pl * a.box_plane, a.box_pitch, pr, q, a.r[i], H, W);
-      __stcs(dS + (long long)pr * a.sat_pitch + q, acc);
-      continue;
-    }
 #pragma unroll
-    for (int i = 0; i < SATGB_MAX_RADII; ++i) {
-      if (i >= a.nr) break;
-      const int r = a.r[i];
-      const float* g = a.box[i] + pl * a.box_plane;
-      const int xp = q - r, xm = q + 1 + r, yp = pr - r, ym = pr + 1 + r;
-      if (pr >= 2 * r && pr <= H - 2 - 2 * r && q >= 2 * r && q <= W - 2 - 2 * r) {
-        // interior: the four outputs with a corner here have whole windows
-        const float* rp = g + (long long)yp * a.box_pitch;
-        const float* rm = g + (long long)ym * a.box_pitch;
-        acc += ((__ldg(rp + xp) - __ldg(rp + xm)) - (__ldg(rm + xp) - __ldg(rm + xm))) *
-               (a.inv_full[i] * a.inv_full[i]);
-        continue;
-      }
-      float t = 0.f;
-      if (yp >= 0) {
-        const float* row = g + (long long)yp * a.box_pitch;
-        float u = ixp[i] != 0.f ? __ldg(row + xp) * ixp[i] : 0.f;
-        if (ixm[i] != 0.f) u -= __ldg(row + xm) * ixm[i];
-        t = u * win(yp, r, H, a.inv_full[i]).inv;
-      }
-      if (ym <= H - 1) {
-        const float* row = g + (long long)ym * a.box_pitch;
-        float u = ixp[i] != 0.f ? __ldg(row + xp) * ixp[i] : 0.f;
-        if (ixm[i] != 0.f) u -= __ldg(row + xm) * ixm[i];
-        t -= u * win(ym, r, H, a.inv_full[i]).inv;
-      }
-      acc += t;
-    }
-    __stcs(dS + (long long)pr * a.sat_pitch + q, acc);
+  for (int k = 0; k < kBRows; ++k) {
+    const int pr = ybase + k * kBY;
+    if (pr < H - 1 && q < W - 1) __stcs(dS + (long long)pr * a.sat_pitch + q, acc[k]);
   }
+}
+
+// The last row and the last column of dS, where the +1 index set of the
+// gather is a range of r + 1 rows or columns: one thread per element, and the
+// corner (H-1, W-1), with (r + 1)^2 taps per radius, summed by one warp.
+constexpr int kEdgeThreads = 256;
+
+template <int NR>
+__global__ void __launch_bounds__(kEdgeThreads) box_bwd_edge_kernel(const __grid_constant__ BoxArgs a) {
+  const int W = (int)a.w, H = (int)a.h;
+  const long long pl = blockIdx.z;
+  float* dS = a.sat + pl * a.sat_plane;
+  const long long e = (long long)blockIdx.x * kEdgeThreads + threadIdx.x;
+  const long long n_edge = (long long)(W - 1) + (H - 1); // the last row and column without the corner
+  if (blockIdx.x == gridDim.x - 1) {
+    if (threadIdx.x < 32) { // the corner
+      float v = 0.f;
+      for (int i = 0; i < NR; ++i)
+        v += adjoint_edge_warp(a.box[i] + pl * a.box_plane, a.box_pitch, H - 1, W - 1, a.r[i], H, W, threadIdx.x);
+      if (threadIdx.x == 0) dS[(long long)(H - 1) * a.sat_pitch + (W - 1)] = v;
+    }
+    return;
+  }
+  if (e >= n_edge) return;
+  const int pr = e < W - 1 ? H - 1 : (int)(e - (W - 1));
+  const int q = e < W - 1 ? (int)e : W - 1;
+  float v = 0.f;
+  for (int i = 0; i < NR; ++i) v += adjoint_edge(a.box[i] + pl * a.box_plane, a.box_pitch, pr, q, a.r[i], H, W);
+  dS[(long long)pr * a.sat_pitch + q] = v;
 }
 
 satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a);
@@ -237,6 +349,7 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
   a.sat_pitch = d->sat_pitch;
   a.sat_plane = d->sat_plane_stride;
   a.nr = d->n_radii;
+  a.rmax = 0;
   a.box_pitch = d->box_pitch;
   a.box_plane = d->box_plane_stride;
   for (int i = 0; i < SATGB_MAX_RADII; ++i) {
@@ -248,6 +361,7 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
     if (d->radius[i] < 0 || !d->d_box[i]) return SATGB_ERR_INVALID_ARG;
     if (((uintptr_t)d->d_box[i] % 4) != 0) return SATGB_ERR_MISALIGNED;
     a.r[i] = d->radius[i];
+    a.rmax = a.r[i] > a.rmax ? a.r[i] : a.rmax;
     a.inv_full[i] = 1.0f / (float)(2 * (double)d->radius[i] + 1);
     a.box[i] = static_cast<float*>(d->d_box[i]);
   }
@@ -262,7 +376,14 @@ extern "C" satgb_status satgb_box_filter_fwd(const satgb_box_desc* d, satgb_stre
   if (st != SATGB_OK || d->width == 0 || d->height == 0 || d->n_planes == 0) return st;
   dim3 grid((unsigned)((d->width + kBX - 1) / kBX), (unsigned)((d->height + kBY * kRows - 1) / (kBY * kRows)),
             (unsigned)d->n_planes);
-  box_fwd_kernel<<<grid, dim3(kBX, kBY), 0, (cudaStream_t)stream>>>(a);
+  const dim3 block(kBX, kBY);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a.nr) {
+    case 1: box_fwd_kernel<1><<<grid, block, 0, s>>>(a); break;
+    case 2: box_fwd_kernel<2><<<grid, block, 0, s>>>(a); break;
+    case 3: box_fwd_kernel<3><<<grid, block, 0, s>>>(a); break;
+    default: box_fwd_kernel<4><<<grid, block, 0, s>>>(a); break;
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return satgb::api_cuda_fail(e, "box_fwd_kernel launch");
   satgb::api_count_launch();
@@ -273,11 +394,30 @@ extern "C" satgb_status satgb_box_filter_bwd(const satgb_box_desc* d, satgb_stre
   BoxArgs a;
   satgb_status st = check_desc(d, a);
   if (st != SATGB_OK || d->width == 0 || d->height == 0 || d->n_planes == 0) return st;
-  dim3 grid((unsigned)((d->width + kBX - 1) / kBX), (unsigned)((d->height + kBY * kRows - 1) / (kBY * kRows)),
+  dim3 grid((unsigned)((d->width + kBX - 1) / kBX), (unsigned)((d->height + kBY * kBRows - 1) / (kBY * kBRows)),
             (unsigned)d->n_planes);
-  box_bwd_kernel<<<grid, dim3(kBX, kBY), 0, (cudaStream_t)stream>>>(a);
-  const cudaError_t e = cudaGetLastError();
+  const dim3 block(kBX, kBY);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (a.nr) {
+    case 1: box_bwd_kernel<1><<<grid, block, 0, s>>>(a); break;
+    case 2: box_bwd_kernel<2><<<grid, block, 0, s>>>(a); break;
+    case 3: box_bwd_kernel<3><<<grid, block, 0, s>>>(a); break;
+    default: box_bwd_kernel<4><<<grid, block, 0, s>>>(a); break;
+  }
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return satgb::api_cuda_fail(e, "box_bwd_kernel launch");
+  satgb::api_count_launch();
+  // the last row and column: (W - 1) + (H - 1) elements a plane, then one block for the corner
+  const dim3 egrid((unsigned)((d->width + d->height - 2 + kEdgeThreads - 1) / kEdgeThreads + 1), 1,
+                   (unsigned)d->n_planes);
+  switch (a.nr) {
+    case 1: box_bwd_edge_kernel<1><<<egrid, kEdgeThreads, 0, s>>>(a); break;
+    case 2: box_bwd_edge_kernel<2><<<egrid, kEdgeThreads, 0, s>>>(a); break;
+    case 3: box_bwd_edge_kernel<3><<<egrid, kEdgeThreads, 0, s>>>(a); break;
+    default: box_bwd_edge_kernel<4><<<egrid, kEdgeThreads, 0, s>>>(a); break;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return satgb::api_cuda_fail(e, "box_bwd_edge_kernel launch");
   satgb::api_count_launch();
   return SATGB_OK;
 }

@@ -146,6 +146,20 @@ def test_box_grad_vs_float64_cumsum(cuda, shape):
     assert float((gx.double() - g64).abs().max()) <= tol
 
 
+@pytest.mark.parametrize("shape,radii", [
+    ((1, 2, 200, 333), (2, 9, 32)),   # staged tiles, the largest staged radius, ragged tiles
+    ((1, 1, 130, 170), (33,)),        # above the staged limit: the per-tap gather
+    ((1, 1, 97, 131), (0, 1, 32, 70)),  # staged radii next to one past every side
+])
+def test_box_grad_tiles_and_large_radii(cuda, shape, radii):
+    g = torch.Generator(device="cpu").manual_seed(25)
+    x = torch.randn(shape, generator=g).to(cuda)
+    wts = torch.randn(shape[:-2] + (len(radii),) + shape[-2:], generator=g).to(cuda)
+    gx, g64 = _grads(x, radii, wts)
+    tol = 1e-4 * max(1.0, float(g64.abs().max()))
+    assert float((gx.double() - g64).abs().max()) <= tol
+
+
 def test_box_grad_central_fd(cuda):
     """64 x 64 crops: the kernel gradient against FP64 central differences
     (h = 1e-3) of the FP64 loss at 24 random pixels."""
