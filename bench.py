@@ -591,9 +591,30 @@ def run_workload(args):
         _, per = _time_steps(step, args.steps, args.warmup, stream, 0.0)
         sat_gb300.stream_check()
         print(json.dumps({"case": args.case, "n": n, "ms_median": round(statistics.median(per), 5)}))
+    elif args.case == "box_parts":
+        # the four launches of the box-filter layer's forward + backward, each timed alone
+        from sat_gb300 import api
+        n = 8 if args.small else 64
+        x, wts, radii = build_box(dev, n=n)
+        s = api.sat(x, torch.float32)
+        gs = api.box_means_adjoint(wts, radii)
+        parts = {"sat": lambda: api.sat(x, torch.float32, out=s),
+                 "box_means": lambda: api.box_means_from_sat(s, radii),
+                 "adjoint": lambda: api.box_means_adjoint(wts, radii, out=gs),
+                 "reverse_sat": lambda: api.sat(gs, torch.float32, reverse=True, out=gs)}
+        plane = x.numel() * 4
+        moved = {"sat": 2 * plane, "box_means": (1 + len(radii)) * plane, "adjoint": (len(radii) + 1) * plane,
+                 "reverse_sat": 2 * plane}
+        res = {"case": args.case, "n": n}
+        for name, fn in parts.items():
+            _, per = _time_steps(fn, args.steps, args.warmup, stream, 0.0)
+            med = statistics.median(per)
+            res[name] = {"ms_median": round(med, 4), "gbs": round(moved[name] / (med / 1e3) / GB, 1)}
+        sat_gb300.stream_check()
+        print(json.dumps(res))
 
 
-WORKLOADS = ("batch512", "batch512_packed", "box_fwd", "box_fwdbwd")
+WORKLOADS = ("batch512", "batch512_packed", "box_fwd", "box_fwdbwd", "box_parts")
 
 
 def main():

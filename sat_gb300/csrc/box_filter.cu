@@ -39,6 +39,7 @@ struct BoxArgs {
   float inv_full[SATGB_MAX_RADII]; // 1 / (2r + 1): the reciprocal window length away from the edges
   float* box[SATGB_MAX_RADII];
   int64_t box_pitch, box_plane;
+  int idx32; // every in-plane element offset fits in 32 bits: only then the interior paths run (int offsets)
 };
 
 // A block covers 32 columns x 64 rows of one plane: blockDim (32, 8), each
@@ -82,23 +83,26 @@ __global__ void __launch_bounds__(kBX * kBY) box_fwd_kernel(const __grid_constan
   const long long pl = blockIdx.z;
   const float* S = a.sat + pl * a.sat_plane;
   const int ybase = blockIdx.y * (kBY * kRows) + threadIdx.y;
-  if (fwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kRows))) {
-    const long long sp = a.sat_pitch, bp = a.box_pitch;
+  if (a.idx32 && fwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kRows))) {
+    const int sp = (int)a.sat_pitch, bp = (int)a.box_pitch;
 #pragma unroll
     for (int i = 0; i < NR; ++i) {
       const int r = a.r[i];
       const float inv2 = a.inv_full[i] * a.inv_full[i];
-      const float* hi = S + (long long)(ybase + r) * sp + x;
-      const float* lo = hi - (long long)(2 * r + 1) * sp;
-      float* B = a.box[i] + pl * a.box_plane + (long long)ybase * bp + x;
+      const int hi = (ybase + r) * sp + x; // in-plane element offsets
+      const int lo = hi - (2 * r + 1) * sp;
+      float* B = a.box[i] + pl * a.box_plane;
+      const int bo = ybase * bp + x;
       float out[kRows];
 #pragma unroll
       for (int k = 0; k < kRows; ++k) {
-        const long long o = (long long)k * kBY * sp;
-        out[k] = ((__ldg(hi + o + r) - __ldg(hi + o - r - 1)) - (__ldg(lo + o + r) - __ldg(lo + o - r - 1))) * inv2;
+        const int o = k * kBY * sp;
+        out[k] = ((__ldg(S + (hi + o + r)) - __ldg(S + (hi + o - r - 1))) -
+                  (__ldg(S + (lo + o + r)) - __ldg(S + (lo + o - r - 1)))) *
+                 inv2;
       }
 #pragma unroll
-      for (int k = 0; k < kRows; ++k) __stcs(B + (long long)k * kBY * bp, out[k]);
+      for (int k = 0; k < kRows; ++k) __stcs(B + (bo + k * kBY * bp), out[k]);
     }
     return;
   }
@@ -220,9 +224,10 @@ __global__ void __launch_bounds__(kBX * kBY, 3) box_bwd_kernel(const __grid_cons
   const int q = blockIdx.x * kBX + threadIdx.x;
   const long long pl = blockIdx.z;
   const int ybase = blockIdx.y * (kBY * kBRows) + threadIdx.y;
-  if (bwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kBRows))) {
-    // dS(p,q) = sum_i c_i ((g(p-r,q-r) - g(p-r,q+1+r)) - (g(p+1+r,q-r) - g(p+1+r,q+1+r)))
-    const long long gp = a.box_pitch;
+  if (a.idx32 && bwd_block_interior(a, blockIdx.x * kBX, blockIdx.y * (kBY * kBRows))) {
+    // dS(p,q) = sum_i c_i ((g(p-r,q-r) - g(p-r,q+1+r)) - (g(p+1+r,q-r) - g(p+1+r,q+1+r))),
+    // with in-plane element offsets in ints
+    const int gp = (int)a.box_pitch;
     float acc[kBRows];
 #pragma unroll
     for (int k = 0; k < kBRows; ++k) acc[k] = 0.f;
@@ -231,17 +236,19 @@ __global__ void __launch_bounds__(kBX * kBY, 3) box_bwd_kernel(const __grid_cons
       const int r = a.r[i];
       const int d = 2 * r + 1;
       const float c = a.inv_full[i] * a.inv_full[i];
-      const float* t = a.box[i] + pl * a.box_plane + (long long)(ybase - r) * gp + (q - r);
-      const float* b = t + (long long)d * gp;
+      const float* g = a.box[i] + pl * a.box_plane;
+      const int t = (ybase - r) * gp + (q - r);
+      const int b = t + d * gp;
 #pragma unroll
       for (int k = 0; k < kBRows; ++k) {
-        const long long o = (long long)k * kBY * gp;
-        acc[k] += ((__ldg(t + o) - __ldg(t + o + d)) - (__ldg(b + o) - __ldg(b + o + d))) * c;
+        const int o = k * kBY * gp;
+        acc[k] += ((__ldg(g + (t + o)) - __ldg(g + (t + o + d))) - (__ldg(g + (b + o)) - __ldg(g + (b + o + d)))) * c;
       }
     }
-    float* dS = a.sat + pl * a.sat_plane + (long long)ybase * a.sat_pitch + q;
+    float* dS = a.sat + pl * a.sat_plane;
+    const int so = ybase * (int)a.sat_pitch + q;
 #pragma unroll
-    for (int k = 0; k < kBRows; ++k) __stcs(dS + (long long)k * kBY * a.sat_pitch, acc[k]);
+    for (int k = 0; k < kBRows; ++k) __stcs(dS + (so + k * kBY * (int)a.sat_pitch), acc[k]);
     return;
   }
   const bool live = q < W;
@@ -350,6 +357,8 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
   a.sat_plane = d->sat_plane_stride;
   a.nr = d->n_radii;
   a.rmax = 0;
+  a.idx32 = (d->height - 1) * d->sat_pitch + d->width < (1LL << 31) &&
+            (d->height - 1) * d->box_pitch + d->width < (1LL << 31);
   a.box_pitch = d->box_pitch;
   a.box_plane = d->box_plane_stride;
   for (int i = 0; i < SATGB_MAX_RADII; ++i) {

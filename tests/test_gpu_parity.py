@@ -274,6 +274,26 @@ def test_batch_plan_float_and_reverse(cuda, oracle):
         plan.close()
 
 
+def test_full_size_u8_properties_and_configs_agree(cuda):
+    """8192 x 8192 u8 -> u32, the reference's largest case: the last row is
+    the prefix of the column sums and the last column the prefix of the row
+    sums (mod 2^32: the total of 2^26 bytes wraps), and the default tiles and
+    the 64-row two-CTA tiles agree bit for bit."""
+    g = torch.Generator(device=cuda).manual_seed(41)
+    x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda, generator=g)
+    s_def = sat_gb300.sat(x, torch.uint32)
+    sat_gb300.set_config(2)
+    try:
+        s2 = sat_gb300.sat(x, torch.uint32)
+    finally:
+        sat_gb300.set_config(-1)
+    assert torch.equal(s_def.view(torch.int32), s2.view(torch.int32))
+    col = x.to(torch.int64).sum(0).cumsum(0) & 0xFFFFFFFF
+    row = x.to(torch.int64).sum(1).cumsum(0) & 0xFFFFFFFF
+    assert torch.equal(s_def[-1].to(torch.int64), col)
+    assert torch.equal(s_def[:, -1].to(torch.int64), row)
+
+
 @pytest.mark.parametrize("cfg", [0, 1, 2, 3])
 def test_timeout_is_reported_and_context_survives(cuda, oracle, cfg):
     """A tile that never publishes makes its dependents hit the wait limit
