@@ -235,7 +235,8 @@ def run_gpu(args):
                        "ms_median": round(statistics.median(per_d), 4)}
     sat_gb300.stream_check()
     # ---- row-only and column-only scans (ScanX / ScanY), f32 8192^2 --------------
-    for nm, fn in (("scan_rows_f32_8192", sat_gb300.scan_rows), ("scan_cols_f32_8192", sat_gb300.scan_cols)):
+    for nm, fn in (("scan_rows_f32_8192", sat_gb300.scan_rows), ("scan_cols_f32_8192", sat_gb300.scan_cols),
+                   ("scan_rows_transposed_f32_8192", sat_gb300.scan_rows_transposed)):
         ms, per_s = _time_steps(lambda: fn(x, torch.float32, out=y), 50, 5, stream, 0.2)
         sub[nm] = {"gbs": round(step_bytes / (statistics.median(per_s) / 1e3) / GB, 1),
                    "ms_median": round(statistics.median(per_s), 4)}
@@ -392,6 +393,8 @@ CASES = {
     "u8_8192": ("uint8", "uint32", "plain", False, 8192, 8192),
     "f64_4096": ("float64", "float64", "plain", False, 4096, 4096),
     "f32r_8192": ("float32", "float32", "plain", True, 8192, 8192),
+    "f32t_8192": ("float32", "float32", "rows_transposed", False, 8192, 8192),
+    "u8t_8192": ("uint8", "uint32", "rows_transposed", False, 8192, 8192),
 }
 
 
@@ -416,7 +419,11 @@ def run_case(args):
     if tout == torch.uint32:
         y = y.view(torch.uint32)
     stream = torch.cuda.current_stream()
-    fn = lambda: sat_gb300.sat(x, tout, mode=mode, reverse=rev, out=y)
+    if mode == "rows_transposed":
+        y = y.t().contiguous() if h != w else y
+        fn = lambda: sat_gb300.scan_rows_transposed(x, tout, out=y)
+    else:
+        fn = lambda: sat_gb300.sat(x, tout, mode=mode, reverse=rev, out=y)
     total, per = _time_steps(fn, args.steps, args.warmup, stream, 0.0)
     sat_gb300.stream_check()
     nbytes = x.numel() * (x.element_size() + y.element_size())

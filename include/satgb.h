@@ -150,6 +150,16 @@ satgb_status satgb_scan_rows(satgb_dtype in_t, satgb_dtype out_t, const void* d_
 satgb_status satgb_scan_cols(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch,
                              void* d_out, int64_t out_pitch, int64_t width, int64_t height, satgb_stream stream);
 
+/* Row scan with transposed output, out(x, y) = sum_{i<=x} in(y, i): the input
+ * is width x height (pitch in_pitch), the output height x width, i.e. width
+ * rows of height elements (pitch out_pitch >= height).  Replaces the
+ * reference's SerielScan::TestX (integralImage/BRLT-Scan.cu:128-190), one
+ * serielScan launch whose output is IntegralImageAllRow transposed.  Same
+ * type pairs as the scans; input and output must not overlap. */
+satgb_status satgb_scan_rows_transposed(satgb_dtype in_t, satgb_dtype out_t, const void* d_in, int64_t in_pitch,
+                                        void* d_out, int64_t out_pitch, int64_t width, int64_t height,
+                                        satgb_stream stream);
+
 /* The same SAT for a stack of n_planes equally sized images (e.g. the N*C
  * planes of an N x C x H x W tensor), plane p starting at d_in + p *
  * in_plane_stride and d_out + p * out_plane_stride (elements); each plane gets

@@ -103,6 +103,7 @@ SIGNATURES = {
     "satgb_version": (_I, []),
     "satgb_sat_planes": (_ST, [ctypes.POINTER(satgb_sat_desc), _I64, _I64, _I64, _P]),
     "satgb_scan_rows": (_ST, [_I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
+    "satgb_scan_rows_transposed": (_ST, [_I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "satgb_scan_cols": (_ST, [_I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "satgb_box_filter_fwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),
     "satgb_box_filter_bwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),

@@ -140,6 +140,27 @@ def scan_cols(src: torch.Tensor, out_dtype=None, out=None, stream=None) -> torch
     return _scan("satgb_scan_cols", src, out_dtype, out, stream)
 
 
+def scan_rows_transposed(src: torch.Tensor, out_dtype=None, out=None, stream=None) -> torch.Tensor:
+    """Row scan with transposed output, out(x, y) = sum_{i<=x} src(y, i): an
+    (H, W) input gives a (W, H) output (SerielScan::TestX, BRLT-Scan.cu:128-190)."""
+    _check_cuda(src)
+    if src.dim() != 2:
+        raise SatError(_lib.ERR_INVALID_ARG, f"an image is a 2-D tensor, got shape {tuple(src.shape)}")
+    if out_dtype is None:
+        out_dtype = out.dtype if out is not None else DEFAULT_OUT.get(src.dtype, src.dtype)
+    shape_t = (src.shape[1], src.shape[0])
+    if out is None:
+        out = torch.empty(shape_t, dtype=out_dtype, device=src.device)
+    elif out.dtype != out_dtype or tuple(out.shape) != shape_t:
+        raise SatError(_lib.ERR_INVALID_ARG, "out has the wrong dtype or shape (it is the transposed shape)")
+    _check_cuda(out)
+    ip, ipitch, w, h = _image_args(src)
+    op, opitch, _, _ = _image_args(out)
+    check(_lib.load().satgb_scan_rows_transposed(dtype_code(src.dtype), dtype_code(out.dtype), ip, ipitch, op, opitch,
+                                                 w, h, _stream_handle(stream)))
+    return out
+
+
 ALGORITHMS = {
     "ScanRow-BRLT": scanrow_brlt,
     "BRLT-ScanRow": brlt_scanrow,

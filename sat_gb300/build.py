@@ -28,6 +28,7 @@ SOURCES = [
     "sat_inst_f32.cu",
     "sat_inst_f64.cu",
     "box_filter.cu",
+    "scan_rows_t.cu",
     "satgb_noalloc.cu",
 ]
 

@@ -58,6 +58,29 @@ def test_validation_errors(satlib, fn):
     assert isinstance(msg, bytes)
 
 
+def test_scan_rows_transposed_validation(satlib):
+    """The transposed row scan's output is height wide and width tall: its
+    pitch is checked against the height, and the buffers may not overlap."""
+    f = satlib.satgb_scan_rows_transposed
+    U8, U32 = _lib.U8, _lib.U32
+
+    def call(in_t=U8, out_t=U32, d_in=0x1000, ip=16, d_out=0x100000, op=8, w=16, h=8):
+        return f(in_t, out_t, d_in, ip, d_out, op, w, h, None)
+
+    assert call(w=-1) == _lib.ERR_INVALID_ARG
+    assert call(d_in=0) == _lib.ERR_INVALID_ARG
+    assert call(ip=15) == _lib.ERR_INVALID_ARG               # in pitch < width
+    assert call(op=7) == _lib.ERR_INVALID_ARG                # out pitch < height
+    assert call(in_t=9) == _lib.ERR_INVALID_ARG
+    assert call(in_t=_lib.U16) == _lib.ERR_UNSUPPORTED_TYPES
+    assert call(in_t=_lib.F32, out_t=U32) == _lib.ERR_UNSUPPORTED_TYPES
+    assert call(d_out=0x100002) == _lib.ERR_MISALIGNED
+    assert call(d_out=0x1008) == _lib.ERR_INVALID_ARG        # overlap
+    assert call(w=1 << 31, ip=1 << 31) == _lib.ERR_OVERFLOW
+    assert call(w=0) == _lib.OK
+    assert call(h=0, d_in=0, d_out=0) == _lib.OK
+
+
 def test_error_string_set_on_failure(satlib):
     assert _call(satlib, "satgb_scanrow_brlt", _lib.U8, _lib.U32, w=-1) == _lib.ERR_INVALID_ARG
     assert b"width" in satlib.satgb_last_error_string()

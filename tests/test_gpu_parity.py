@@ -420,6 +420,43 @@ def test_row_and_column_scans_all_pairs(cuda, oracle, which):
                 assert err.max() <= TOL[np.dtype(to)], (which, name, shape, err.max())
 
 
+def test_scan_rows_transposed_all_pairs(cuda, oracle):
+    """satgb_scan_rows_transposed (SerielScan::TestX: IntegralImageAllRow, then
+    Transpose) against the oracle's row scan, transposed: bit-exact for integer
+    outputs, floats within the scans' tolerance."""
+    for name, (ti, to) in oracle.PAIRS.items():
+        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (33, 129), (129, 257), (517, 769)]):
+            a = oracle.gen(PAIR_KINDS[ti], 3500 + i, shape)
+            out = to_np(sat_gb300.scan_rows_transposed(to_dev(a), SCAN_TORCH[np.dtype(to)]))
+            assert out.shape == (shape[1], shape[0])
+            if np.dtype(to).kind in "iu":
+                assert np.array_equal(bits(out), bits(oracle.scan_rows(a, to).T)), (name, shape)
+            else:
+                exact = np.cumsum(a.astype(np.float64), axis=1).T
+                den = np.cumsum(np.abs(a.astype(np.float64)), axis=1).T
+                err = np.abs(out.astype(np.float64) - exact) / np.maximum(den, 1e-300)
+                assert err.max() <= TOL[np.dtype(to)], (name, shape, err.max())
+
+
+def test_scan_rows_transposed_pitched_and_full_size(cuda, oracle):
+    """Pitched input and output, odd pitches (no vector loads), and an
+    8192 x 8192 u8 -> u32 check: the last output row is every input row's sum
+    and the output equals the transposed row scan, mod 2^32."""
+    a = oracle.gen("u8", 92, (333, 555))
+    src = empty_pitched(333, 555, 641, torch.uint8)
+    src.copy_(to_dev(a))
+    dst = empty_pitched(555, 333, 400, torch.uint32, fill=-1)
+    sat_gb300.scan_rows_transposed(src, torch.uint32, out=dst)
+    assert np.array_equal(to_np(dst), oracle.scan_rows(a, np.uint32).T)
+    g = torch.Generator(device=cuda).manual_seed(43)
+    x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda, generator=g)
+    t = sat_gb300.scan_rows_transposed(x, torch.uint32)
+    r = sat_gb300.scan_rows(x, torch.uint32)
+    assert torch.equal(t.view(torch.int32), r.view(torch.int32).t())
+    rows = x.to(torch.int64).sum(1) & 0xFFFFFFFF
+    assert torch.equal(t[-1].to(torch.int64), rows)
+
+
 def test_scans_pitched_and_full_size(cuda, oracle):
     """Pitched u8 -> u32 rows and columns, and an 8192 x 8192 check of
     sum(row scan) == sum(column scan) == the SAT's last element, mod 2^32."""
