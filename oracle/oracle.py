@@ -230,6 +230,45 @@ def ref_serial(a: np.ndarray, out_dtype) -> Optional[np.ndarray]:
     return out
 
 
+def _ref_scan(kind: str, a: np.ndarray, out_dtype) -> Optional[np.ndarray]:
+    R = ref_lib()
+    if R is None:
+        return None
+    h, w = a.shape
+    a = np.ascontiguousarray(a)
+    name = pair_name(a.dtype, out_dtype)
+    if kind == "allrow_t":
+        tmp = np.zeros((h, w), dtype=out_dtype)
+        out = np.zeros((w, h), dtype=out_dtype)
+        f = getattr(R, f"ref_allrow_t_{name}")
+        f.argtypes = [_P, _P, _P, ctypes.c_int, ctypes.c_int]
+        f.restype = None
+        f(_ptr(a), _ptr(tmp), _ptr(out), w, h)
+        return out
+    out = np.zeros((h, w), dtype=out_dtype)
+    f = getattr(R, f"ref_{kind}_{name}")
+    f.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int]
+    f.restype = None
+    f(_ptr(a), _ptr(out), w, h)
+    return out
+
+
+def ref_scan_rows(a: np.ndarray, out_dtype) -> Optional[np.ndarray]:
+    """The reference's own IntegralImageAllRow, or None where it is not built."""
+    return _ref_scan("allrow", a, out_dtype)
+
+
+def ref_scan_rows_transposed(a: np.ndarray, out_dtype) -> Optional[np.ndarray]:
+    """The reference's IntegralImageAllRow followed by its Transpose (the check
+    of SerielScan::TestX), a (W, H) array, or None where it is not built."""
+    return _ref_scan("allrow_t", a, out_dtype)
+
+
+def ref_scan_cols(a: np.ndarray, out_dtype) -> Optional[np.ndarray]:
+    """The reference's own IntegralStride down every column, or None."""
+    return _ref_scan("colscan", a, out_dtype)
+
+
 def ref_parallel(a: np.ndarray) -> Optional[np.ndarray]:
     """The reference's own IntegralImageParallel<T,T> (matching types only)."""
     R = ref_lib()

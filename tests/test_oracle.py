@@ -142,3 +142,22 @@ def test_oracle_row_and_column_scans(oracle):
         with np.errstate(over="ignore"):
             assert np.array_equal(oracle.scan_rows(a, to).view(np.uint32), np.cumsum(acc, axis=1, dtype=np.uint32))
             assert np.array_equal(oracle.scan_cols(a, to).view(np.uint32), np.cumsum(acc, axis=0, dtype=np.uint32))
+
+
+def test_reference_live_scans_match_port(oracle):
+    """The row scan, the transposed row scan and the column scan of the
+    restatement against the reference's own IntegralImageAllRow,
+    AllRow + Transpose (SerielScan::TestX's check) and IntegralStride, bit for
+    bit, every pair (floats included: the same order of additions)."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference CPU code not built here (no reference checkout)")
+    kinds = {np.uint8: "u8", np.int8: "i8", np.int32: "i32", np.uint32: "u32",
+             np.float32: "f32u", np.float64: "f64u"}
+    for name, (ti, to) in oracle.PAIRS.items():
+        for shape in [(1, 1), (5, 300), (300, 5), (129, 131)]:
+            a = oracle.gen(kinds[ti], 23, shape)
+            rows = oracle.scan_rows(a, to)
+            assert np.array_equal(_bits(oracle.ref_scan_rows(a, to)), _bits(rows)), (name, shape)
+            assert np.array_equal(_bits(oracle.ref_scan_rows_transposed(a, to)),
+                                  _bits(np.ascontiguousarray(rows.T))), (name, shape)
+            assert np.array_equal(_bits(oracle.ref_scan_cols(a, to)), _bits(oracle.scan_cols(a, to))), (name, shape)
