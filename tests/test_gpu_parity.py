@@ -274,6 +274,25 @@ def test_batch_plan_float_and_reverse(cuda, oracle):
         plan.close()
 
 
+def test_autotune_records_and_results_stay_exact(cuda, oracle, tmp_path, monkeypatch):
+    """satgb_autotune times every configuration on the caller's buffers, picks
+    one, writes it to the tuning cache (one JSON object per line) and the
+    next call with that size, which now uses it, is still bit-exact."""
+    import json
+    cache = tmp_path / "tune.jsonl"
+    monkeypatch.setenv("SATGB_TUNE_CACHE", str(cache))
+    a = oracle.gen("u8", 55, (700, 900))
+    x = to_dev(a)
+    y = torch.empty((700, 900), dtype=torch.int32, device=cuda).view(torch.uint32)
+    best = sat_gb300.autotune(x, y)
+    assert 0 <= best < len(sat_gb300.config_names())
+    entries = [json.loads(line) for line in cache.read_text().splitlines()]
+    mine = [e for e in entries if (e["in"], e["out"], e["wb"], e["hb"]) == (_lib.U8, _lib.U32, 10, 10)]
+    assert mine and all(e["cfg"] == best for e in mine)
+    out = to_np(sat_gb300.sat(x, torch.uint32))
+    assert np.array_equal(bits(out), bits(oracle.sat_serial(a, np.uint32)))
+
+
 def test_full_size_u8_properties_and_configs_agree(cuda):
     """8192 x 8192 u8 -> u32, the reference's largest case: the last row is
     the prefix of the column sums and the last column the prefix of the row
