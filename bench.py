@@ -331,10 +331,31 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the baseline's record."""
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_baseline(seconds: float):
-    """The reference's CPU integral image (oracle restatement of
-    IntegralImageParallel, OpenMP over all host cores) on the headline
-    workload, repeated for about `seconds` of CPU time."""
+    """The reference's CPU integral image on the headline workload: the
+    restatement of IntegralImageParallel (OpenMP over all host cores),
+    repeated for about `seconds` of CPU time, and IntegralImageSerial on one
+    core, a bounded sample of whole images."""
     import numpy as np
     from oracle import oracle as O
     O.build(with_ref=False)
@@ -349,8 +370,19 @@ def cpu_baseline(seconds: float):
         if time.time() - t0 >= seconds:
             break
     dt = (time.time() - t0) / reps
+    t0 = time.time()
+    sreps = 0
+    while True:
+        O.sat_serial(a, np.float32)
+        sreps += 1
+        if time.time() - t0 >= min(seconds, 3.0):
+            break
+    sdt = (time.time() - t0) / sreps
     return {"value": round(a.size * 8 / dt / GB, 3), "unit": "GB/s", "cores": n, "kind": "port",
-            "sample": f"{reps} full 8192x8192 f32 SATs with IntegralImageParallel (row pass then column pass), {n} OpenMP threads"}
+            "sample": f"{reps} full 8192x8192 f32 SATs with IntegralImageParallel (row pass then column pass), {n} OpenMP threads",
+            "serial_1core": {"value": round(a.size * 8 / sdt / GB, 3), "unit": "GB/s", "cores": 1,
+                             "sample": f"{sreps} full 8192x8192 f32 SATs with IntegralImageSerial"},
+            "cpu_model": cpu_model()}
 
 
 def run_reference(args):
