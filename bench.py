@@ -423,6 +423,11 @@ CASES = {
     "f32_8192": ("float32", "float32", "plain", False, 8192, 8192),
     "f32c_8192": ("float32", "float32", "compensated", False, 8192, 8192),
     "u8_8192": ("uint8", "uint32", "plain", False, 8192, 8192),
+    "u8_2048": ("uint8", "uint32", "plain", False, 2048, 2048),
+    "u8_4096": ("uint8", "uint32", "plain", False, 4096, 4096),
+    "u8_16384": ("uint8", "uint32", "plain", False, 16384, 16384),
+    "u8_32768": ("uint8", "uint32", "plain", False, 32768, 32768),
+    "u8r_8192": ("uint8", "uint32", "plain", True, 8192, 8192),
     "f64_4096": ("float64", "float64", "plain", False, 4096, 4096),
     "f32r_8192": ("float32", "float32", "plain", True, 8192, 8192),
     "f32t_8192": ("float32", "float32", "rows_transposed", False, 8192, 8192),

@@ -11,37 +11,40 @@ namespace satgb {
 
 // Raises the kernel's dynamic shared-memory limit on the current device (once
 // per device); must precede occupancy queries and launches.
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat,
+          bool DIRECT = false>
 cudaError_t prepare_impl() {
-  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB, DIRECT>;
   constexpr int kMaxDev = 64;
   static std::atomic<int> done[kMaxDev];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
-  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
+  e = cudaFuncSetAttribute(&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
   if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
   return e;
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat,
+          bool DIRECT = false>
 cudaError_t launch_impl(const SatParams& p, int grid, cudaStream_t s) {
-  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
-  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>();
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB, DIRECT>;
+  cudaError_t e = prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT>();
   if (e != cudaSuccess) return e;
-  sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
   return cudaGetLastError();
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat,
+          bool DIRECT = false>
 Variant make_variant(int in_t, int out_t, int mode, int cfg) {
-  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB, DIRECT>;
   return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
-                 &launch_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
-                 &prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
-                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND>,
+                 &launch_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT>,
+                 &prepare_impl<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT>,
+                 (const void*)&sat_tile_kernel<TIn, TOut, A, REV, RPW, NW, MINB, KIND, DIRECT>,
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
@@ -134,6 +137,7 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
 //   1: pipelined, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
 //   2: pipelined, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
 //   3: registers, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
+//   4: (1-byte inputs, 4-byte sums only, SG_TALL) pipelined, 256-row tiles, direct stores
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_WS_RPW(A) (sizeof(A) == 8 ? 8 : 4)  /* 64-row tiles either way: */
@@ -153,6 +157,12 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
 #define SG_SCANS(TIN, TOUT, A, IT, OT)                                                                       \
   satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindRows>(IT, OT, SG_MODE_ROWS, 1), \
       satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindCols>(IT, OT, SG_MODE_COLS, 1)
+
+// configuration 4, for 1-byte inputs with 4-byte sums: the pipelined kernel
+// with 256-row tiles (16 warps x 16 rows) and direct stores, both directions
+#define SG_TALL(TIN, TOUT, A, IT, OT)                                                      \
+  satgb::make_variant<TIN, TOUT, A, false, 16, 16, 1, satgb::kKindSat, true>(IT, OT, 0, 4), \
+      satgb::make_variant<TIN, TOUT, A, true, 16, 16, 1, satgb::kKindSat, true>(IT, OT, 0, 4)
 
 #define SG_TABLE(NAME, ...)                                   \
   namespace satgb {                                           \

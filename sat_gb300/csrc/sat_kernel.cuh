@@ -475,13 +475,16 @@ __device__ __forceinline__ ImageView image_view(const SatParams& P, int img) {
   return v;
 }
 
-template <class TIn, class TOut, class A, int RPW, int NW, int CTAS>
+// DIRECT: results go from registers straight to global memory, so a stage
+// holds only the tile's input (tall tiles of 1-byte pixels then fit).
+template <class TIn, class TOut, class A, int RPW, int NW, int CTAS, bool DIRECT = false>
 struct TileShape {
   static constexpr int CPT = 16 / (int)sizeof(TOut);
   static constexpr int TW = 32 * CPT;
   static constexpr int TH = NW * RPW;
   static constexpr int IN_BYTES = TH * TW * (int)sizeof(TIn); // what the TMA load brings
-  static constexpr int STAGE_BYTES = TH * TW * (int)(sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
+  static constexpr int STAGE_BYTES =
+      TH * TW * (int)(DIRECT || sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
   // static shared memory of the kernel (s_tr, s_colp, the vectors), roughly
   // rows per transpose pass: two passes when two CTAs share an SM, to halve the scratch
   static constexpr int RP = (CTAS == 2 && RPW == 8) ? 4 : RPW;
@@ -620,9 +623,10 @@ constexpr int kKindSat = 0;
 constexpr int kKindRows = 1;
 constexpr int kKindCols = 2;
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat,
+          bool DIRECT = false>
 __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_constant__ SatParams P) {
-  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB>;
+  using SH = TileShape<TIn, TOut, A, RPW, NW, MINB, DIRECT>;
   constexpr int CPT = SH::CPT;
   constexpr int TW = SH::TW;
   constexpr int TH = SH::TH;
@@ -641,7 +645,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   constexpr int LPR = 32 / RP;       // transpose-scan: lanes per row ...
   constexpr int CH = RP;             // ... and values per lane
   constexpr int K = Ar<A>::K;
-  constexpr bool WIDEN = sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
+  constexpr bool WIDEN = !DIRECT && sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
   constexpr int ORDER = KIND == kKindCols ? kOrderRows : KIND == kKindRows ? kOrderCols : kOrderDiag;
   using AR = Ar<A>;
 
@@ -1039,9 +1043,13 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
             o.e[c] = OutCvt<TOut, A>::out(KIND == kKindRows ? run : top[c]);
           }
         }
-        *reinterpret_cast<uint4*>(so + r * TW) = o.v;
+        if (DIRECT) {
+          if (y0 + warp * RPW + r < height && nvalid > 0) store_seg<TOut, CPT>(out + r * out_pitch, vout, nvalid, o.e);
+        } else {
+          *reinterpret_cast<uint4*>(so + r * TW) = o.v;
+        }
       }
-      if (!tma_out || tail_out) {
+      if (!DIRECT && (!tma_out || tail_out)) {
         // no TMA for this image, or columns past the map: plain stores
         const long long rows = height - (y0 + warp * RPW);
         const int c0 = tma_out ? (int)(D.tma_out_w - xt > 0 ? D.tma_out_w - xt : 0) : 0;
@@ -1054,7 +1062,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       // generic proxy and next read or overwritten by TMA: order the two.
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncthreads();
-      if (tma_out && tid == PT) {
+      if (!DIRECT && tma_out && tid == PT) {
         const CUtensorMap* map = (P.n_images == 1) ? &P.img0.tmap_out : &P.images[cur.img].tmap_out;
         tma_store_3d(map, cur.tx * TW, cur.ty * TH, cur.p, smem_u32(stages + st * STAGE_ELEMS));
       }

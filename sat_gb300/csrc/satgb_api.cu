@@ -30,6 +30,7 @@ const TileConfig kConfigs[kNumConfigs] = {
     {8, 16, "pipelined: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
     {8, 8, "pipelined: 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs per SM"},
     {8, 16, "registers: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
+    {16, 16, "pipelined, 256-row tiles, direct stores (1-byte inputs, 4-byte sums)"},
 };
 
 namespace {
@@ -418,7 +419,10 @@ int sms_of(int dev) {
 // Compensated f32: the 64-row register tiles (their arithmetic dominates).
 // f64 outputs (slow FP64 adds on GB300): the warp-specialized tiles, whose
 // compute warps never wait at a CTA barrier.
-int default_config(long long width, long long height, int sms, int out_sz, bool compensated) {
+// 1-byte inputs with 4-byte sums: the 256-row direct-store tiles from 2048²
+// up (measured +10 % at 2048², +23 % at 8192², +27 % at 32768² over the
+// 128-row tiles).
+int default_config(long long width, long long height, int sms, int in_sz, int out_sz, bool compensated) {
   const int cpt = 16 / out_sz;
   const long long tw = 32LL * cpt;
   const long long ntx = (width + tw - 1) / tw;
@@ -427,6 +431,7 @@ int default_config(long long width, long long height, int sms, int out_sz, bool 
   const bool large = tiles128 >= 8LL * sms;
   if (out_sz == 8) return large ? 0 : 2;
   if (compensated) return large ? 3 : 2;
+  if (in_sz == 1 && ntx * ((height + 255) / 256) >= 64) return 4;
   return large ? 1 : 2;
 }
 
@@ -436,7 +441,7 @@ int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, lo
   const int sms = sms_of(dev);
   auto it = g_tune.find(TuneKey(in_t, out_t, mode, dir, log2_bucket(w), log2_bucket(h), sms));
   if (it != g_tune.end()) return it->second;
-  return default_config(w, h, sms, (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED);
+  return default_config(w, h, sms, (int)dtype_size(in_t), (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED);
 }
 
 satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const ImageDesc& img0,
@@ -513,6 +518,10 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
             : (mode >= kModeRows) ? 1
                                   : choose_config_locked(in_t, out_t, mode, dir, width, height * std::max(1LL, planes), dev);
   const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
+  if (!v && mode < kModeRows) // a configuration this pair does not have: the untuned choice
+    v = find_variant(in_t, out_t, mode, dir,
+                     default_config(width, height * std::max(1LL, planes), sms_of(dev), (int)in_sz, (int)out_sz,
+                                    mode == SATGB_MODE_COMPENSATED));
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
   ImageDesc d;

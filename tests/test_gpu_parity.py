@@ -89,7 +89,7 @@ SHAPES = [(1, 1), (1, 700), (700, 1), (2, 3), (63, 127), (64, 128), (65, 129), (
           (129, 257), (300, 1000), (1000, 300), (517, 769)]
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 4])
 def test_all_pairs_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -103,7 +103,7 @@ def test_all_pairs_all_configs(cuda, oracle, cfg):
         sat_gb300.set_config(-1)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 4])
 def test_reverse_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -296,24 +296,25 @@ def test_autotune_records_and_results_stay_exact(cuda, oracle, tmp_path, monkeyp
 def test_full_size_u8_properties_and_configs_agree(cuda):
     """8192 x 8192 u8 -> u32, the reference's largest case: the last row is
     the prefix of the column sums and the last column the prefix of the row
-    sums (mod 2^32: the total of 2^26 bytes wraps), and the default tiles and
-    the 64-row two-CTA tiles agree bit for bit."""
+    sums (mod 2^32: the total of 2^26 bytes wraps), and the default tiles, the
+    64-row two-CTA tiles and the 256-row direct-store tiles agree bit for bit."""
     g = torch.Generator(device=cuda).manual_seed(41)
     x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda, generator=g)
     s_def = sat_gb300.sat(x, torch.uint32)
-    sat_gb300.set_config(2)
-    try:
-        s2 = sat_gb300.sat(x, torch.uint32)
-    finally:
-        sat_gb300.set_config(-1)
-    assert torch.equal(s_def.view(torch.int32), s2.view(torch.int32))
+    for cfg in (2, 4):
+        sat_gb300.set_config(cfg)
+        try:
+            s2 = sat_gb300.sat(x, torch.uint32)
+        finally:
+            sat_gb300.set_config(-1)
+        assert torch.equal(s_def.view(torch.int32), s2.view(torch.int32)), cfg
     col = x.to(torch.int64).sum(0).cumsum(0) & 0xFFFFFFFF
     row = x.to(torch.int64).sum(1).cumsum(0) & 0xFFFFFFFF
     assert torch.equal(s_def[-1].to(torch.int64), col)
     assert torch.equal(s_def[:, -1].to(torch.int64), row)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_timeout_is_reported_and_context_survives(cuda, oracle, cfg):
     """A tile that never publishes makes its dependents hit the wait limit
     (every kernel: warp-specialized, pipelined, register-resident); the call
