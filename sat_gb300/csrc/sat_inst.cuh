@@ -136,7 +136,9 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
 //      accumulators) + column, row and store warps
 //   1: pipelined, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
 //   2: pipelined, 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs
-//   3: registers, 128-row tiles (64 for 8-byte accumulators), 16 warps, 1 CTA
+//   3: registers, 128-row tiles, 16 warps, 1 CTA (for 8-byte accumulators too:
+//      the compensated f32 SAT measured 0.284 ms with 64-row and 0.217 ms with
+//      128-row tiles at 8192^2)
 //   4: (1-byte inputs, 4-byte sums only, SG_TALL) pipelined, 256-row tiles, direct stores
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
@@ -146,7 +148,7 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
   satgb::make_variant_ws<TIN, TOUT, A, REV, SG_WS_RPW(A), SG_WS_NWC(A)>(IT, OT, MODE, 0), \
       satgb::make_variant<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),    \
       satgb::make_variant<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 2),       \
-      satgb::make_variant_r<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 3)
+      satgb::make_variant_r<TIN, TOUT, A, REV, 8, 16, 1>(IT, OT, MODE, 3)
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
   SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
 

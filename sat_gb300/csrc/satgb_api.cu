@@ -29,7 +29,7 @@ const TileConfig kConfigs[kNumConfigs] = {
     {4, 16, "warp-specialized: 64-row tiles, 16 compute warps, column/row look-back and store warps"},
     {8, 16, "pipelined: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
     {8, 8, "pipelined: 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs per SM"},
-    {8, 16, "registers: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
+    {8, 16, "registers: 128-row tiles, 16 warps"},
     {16, 16, "pipelined, 256-row tiles, direct stores (1-byte inputs, 4-byte sums)"},
 };
 
@@ -416,7 +416,7 @@ int sms_of(int dev) {
 // Untuned choice, from measurements on GB300 at 8192^2 (f32) and 4096^2 (f64).
 // 4-byte accumulators: the 128-row pipelined tiles when there are enough of
 // them to fill the GPU a few times over, else the 64-row two-CTA tiles.
-// Compensated f32: the 64-row register tiles (their arithmetic dominates).
+// Compensated f32: the 128-row register tiles.
 // f64 outputs (slow FP64 adds on GB300): the warp-specialized tiles, whose
 // compute warps never wait at a CTA barrier.
 // 1-byte inputs with 4-byte sums: the 256-row direct-store tiles from 2048²
