@@ -611,7 +611,9 @@ __device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, 
 //        Top_w(x) = corner + RL(above the warp) + sum_{x0<=i<=x} (colabove(i) + C_w(i)),
 //     then walks its rows once: run = rowleft(y) + E(y) + in-thread row
 //     prefix, acc(x) += run.  Results go back into the tile's stage and leave
-//     by one TMA store (or by plain stores for images TMA cannot address).
+//     by one TMA store (or by plain stores for images TMA cannot address);
+//     with DIRECT they go from registers straight to global memory, one
+//     16-byte segment per thread and row, and the stages hold input only.
 //
 // The reverse (suffix) SAT runs every scan in the opposite direction.
 // ---------------------------------------------------------------------------
