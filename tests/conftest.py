@@ -34,6 +34,14 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_scans():
+    """The reference's own row, transposed-row and column scans on seeded inputs."""
+    z = np.load(os.path.join(os.path.dirname(GOLDEN), "scans_golden.npz"))
+    meta = json.loads(bytes(z["__meta__"]).decode())
+    return z, meta
+
+
+@pytest.fixture(scope="session")
 def satlib():
     from sat_gb300 import build as B
     B.build()

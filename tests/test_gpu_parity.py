@@ -481,6 +481,29 @@ def test_scan_rows_transposed_pitched_and_full_size(cuda, oracle):
     assert torch.equal(t[-1].to(torch.int64), rows)
 
 
+def test_golden_scans(cuda, golden_scans):
+    """The CUDA row, transposed-row and column scans against the reference's
+    own outputs (tests/golden/scans_golden.npz): bit-exact for integer outputs;
+    floats within the scans' tolerance of the reference's sequential sums."""
+    z, meta = golden_scans
+    fns = (("__rows", sat_gb300.scan_rows, 1), ("__rows_t", sat_gb300.scan_rows_transposed, 1),
+           ("__cols", sat_gb300.scan_cols, 0))
+    for case in meta:
+        a = z[case["key"] + "__in"]
+        x = to_dev(a)
+        for suffix, fn, axis in fns:
+            ref = z[case["key"] + suffix]
+            out = to_np(fn(x, SCAN_TORCH[ref.dtype]))
+            if ref.dtype.kind in "iu":
+                assert np.array_equal(bits(out), bits(ref)), (case["key"], suffix)
+            else:
+                den = np.cumsum(np.abs(a.astype(np.float64)), axis=axis)
+                if suffix == "__rows_t":
+                    den = den.T
+                err = np.abs(out.astype(np.float64) - ref.astype(np.float64)) / np.maximum(den, 1e-300)
+                assert err.max() <= TOL[ref.dtype], (case["key"], suffix, err.max())
+
+
 def test_scans_pitched_and_full_size(cuda, oracle):
     """Pitched u8 -> u32 rows and columns, and an 8192 x 8192 check of
     sum(row scan) == sum(column scan) == the SAT's last element, mod 2^32."""

@@ -161,3 +161,17 @@ def test_reference_live_scans_match_port(oracle):
             assert np.array_equal(_bits(oracle.ref_scan_rows_transposed(a, to)),
                                   _bits(np.ascontiguousarray(rows.T))), (name, shape)
             assert np.array_equal(_bits(oracle.ref_scan_cols(a, to)), _bits(oracle.scan_cols(a, to))), (name, shape)
+
+
+def test_golden_scans_bit_exact(oracle, golden_scans):
+    """The restatement's row, transposed-row and column scans against the
+    reference's own outputs (tests/golden/scans_golden.npz), every pair, bit
+    for bit."""
+    z, meta = golden_scans
+    for case in meta:
+        a = z[case["key"] + "__in"]
+        to = z[case["key"] + "__rows"].dtype
+        rows = oracle.scan_rows(a, to)
+        assert np.array_equal(_bits(rows), _bits(z[case["key"] + "__rows"])), case["key"]
+        assert np.array_equal(_bits(np.ascontiguousarray(rows.T)), _bits(z[case["key"] + "__rows_t"])), case["key"]
+        assert np.array_equal(_bits(oracle.scan_cols(a, to)), _bits(z[case["key"] + "__cols"])), case["key"]
