@@ -185,7 +185,8 @@ extern "C" satgb_status satgb_scan_rows_transposed(satgb_dtype in_t, satgb_dtype
   if (in_pitch < width || out_pitch < height)
     return satgb::api_fail(SATGB_ERR_INVALID_ARG,
                            "scan_rows_transposed: in pitch below the width or out pitch below the height");
-  if (width >= (1LL << 31) || height >= (1LL << 31) || height - 1 > INT64_MAX / 16 / in_pitch ||
+  // column and row indices are ints in the kernel, and the tile loop steps past the last column
+  if (width > (1LL << 31) - 2 * kTileW || height > (1LL << 31) - 2 * kStrip || height - 1 > INT64_MAX / 16 / in_pitch ||
       width - 1 > INT64_MAX / 16 / out_pitch)
     return satgb::api_fail(SATGB_ERR_OVERFLOW, "scan_rows_transposed: image too large");
   if (((uintptr_t)d_in % si) != 0 || ((uintptr_t)d_out % so) != 0)
