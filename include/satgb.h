@@ -174,6 +174,7 @@ satgb_status satgb_sat_planes(const satgb_sat_desc* desc, int64_t n_planes, int6
 /* image, read from the inclusive SAT S of the input by four corners:         */
 /*   (S(yb,xb) - S(ya-1,xb) - S(yb,xa-1) + S(ya-1,xa-1)) / area.              */
 /* Up to four radii are filtered in one pass over n_planes planes.            */
+/* Limits: width <= 2^30, height <= 65535 * 32, n_planes <= 65535; f32 only.  */
 /* ------------------------------------------------------------------------- */
 #define SATGB_MAX_RADII 4
 typedef struct {

@@ -343,8 +343,8 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
   if (d->n_radii < 1 || d->n_radii > SATGB_MAX_RADII) return SATGB_ERR_INVALID_ARG;
   if (d->width == 0 || d->height == 0 || d->n_planes == 0) return SATGB_OK;
   if (!d->d_sat || d->sat_pitch < d->width || d->box_pitch < d->width) return SATGB_ERR_INVALID_ARG;
-  // in-plane coordinates are 32-bit; grid.y and grid.z limits
-  if (d->width > (1LL << 30) || d->height > (1LL << 22) || d->n_planes > 65535) return SATGB_ERR_INVALID_ARG;
+  // in-plane coordinates are 32-bit; grid.y (32-row blocks of the backward) and grid.z limits
+  if (d->width > (1LL << 30) || d->height > 65535LL * kBY * kBRows || d->n_planes > 65535) return SATGB_ERR_INVALID_ARG;
   if (d->n_planes > 1 && (d->sat_plane_stride < (d->height - 1) * d->sat_pitch + d->width ||
                           d->box_plane_stride < (d->height - 1) * d->box_pitch + d->width))
     return SATGB_ERR_INVALID_ARG;

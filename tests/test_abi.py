@@ -81,6 +81,36 @@ def test_scan_rows_transposed_validation(satlib):
     assert call(h=0, d_in=0, d_out=0) == _lib.OK
 
 
+def test_box_filter_validation(satlib):
+    """Box-filter descriptors are checked before any launch: radii count and
+    sign, sizes within the launch grid (height up to 65535 x 32), plane count,
+    pitches, alignment; empty sizes are a no-op."""
+    def desc(**kw):
+        d = _lib.satgb_box_desc()
+        d.width, d.height, d.n_planes = kw.get("w", 64), kw.get("h", 64), kw.get("planes", 1)
+        d.d_sat, d.sat_pitch, d.sat_plane_stride = kw.get("sat", 0x10000), kw.get("sp", 64), 64 * 64
+        d.n_radii = kw.get("n", 1)
+        d.radius[0] = kw.get("r", 3)
+        d.d_box[0] = kw.get("box", 0x200000)
+        d.box_pitch, d.box_plane_stride = kw.get("bp", 64), 64 * 64
+        return d
+
+    for fn in (satlib.satgb_box_filter_fwd, satlib.satgb_box_filter_bwd):
+        call = lambda **kw: fn(ctypes.byref(desc(**kw)), None)  # noqa: E731
+        assert call(n=0) == _lib.ERR_INVALID_ARG
+        assert call(n=5) == _lib.ERR_INVALID_ARG
+        assert call(r=-1) == _lib.ERR_INVALID_ARG
+        assert call(h=65535 * 32 + 1) == _lib.ERR_INVALID_ARG
+        assert call(w=(1 << 30) + 1, sp=(1 << 30) + 1, bp=(1 << 30) + 1) == _lib.ERR_INVALID_ARG
+        assert call(planes=65536) == _lib.ERR_INVALID_ARG
+        assert call(sp=63) == _lib.ERR_INVALID_ARG
+        assert call(sat=0) == _lib.ERR_INVALID_ARG
+        assert call(box=0) == _lib.ERR_INVALID_ARG
+        assert call(sat=0x10002) == _lib.ERR_MISALIGNED
+        assert call(box=0x200002) == _lib.ERR_MISALIGNED
+        assert call(w=0) == _lib.OK and call(h=0) == _lib.OK and call(planes=0) == _lib.OK
+
+
 def test_error_string_set_on_failure(satlib):
     assert _call(satlib, "satgb_scanrow_brlt", _lib.U8, _lib.U32, w=-1) == _lib.ERR_INVALID_ARG
     assert b"width" in satlib.satgb_last_error_string()
