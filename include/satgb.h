@@ -175,6 +175,8 @@ satgb_status satgb_sat_planes(const satgb_sat_desc* desc, int64_t n_planes, int6
 /*   (S(yb,xb) - S(ya-1,xb) - S(yb,xa-1) + S(ya-1,xa-1)) / area.              */
 /* Up to four radii are filtered in one pass over n_planes planes.            */
 /* Limits: width <= 2^30, height <= 65535 * 32, n_planes <= 65535; f32 only.  */
+/* Radii >= 0; a radius above max(width, height) - 1 filters like that radius */
+/* (its window already covers the whole image).                               */
 /* ------------------------------------------------------------------------- */
 #define SATGB_MAX_RADII 4
 typedef struct {
@@ -201,13 +203,15 @@ satgb_status satgb_box_filter_bwd(const satgb_box_desc* desc, satgb_stream strea
  * reference.  It calls no cudaMalloc/cudaFree: its look-back scratch is a
  * fixed 16 MiB array inside libsatgb.so that every GPU loading the library
  * holds until the process exits.  Images whose scratch does not fit are
- * rejected with SATGB_ERR_INVALID_ARG: with the 128-row tiles this entry
- * point uses, the array holds 8,160 tiles of 128 x 128 pixels for plain
- * 4-byte outputs (e.g. 8192 x 16256), 4,080 for compensated f32 and 5,433
- * tiles of 128 x 64 pixels for f64 outputs.  The first call on each device looks up the array's
- * device address and should come before any stream capture.  All calls share
- * the array: calls whose kernels overlap on the GPU race and give wrong
- * results.  Device-side wait timeouts are not reported by this entry point. */
+ * rejected with SATGB_ERR_INVALID_ARG (the message gives both sizes): with
+ * the tiles this entry point uses, the array holds 8,160 tiles of 128 x 128
+ * pixels for plain 4-byte outputs (e.g. 10240 x 13056, or 8192 x 16256),
+ * 5,433 tiles of 128 x 64 (width x height) for compensated f32 and 8,128
+ * tiles of 64 x 64 for f64 outputs.  The first call on each device looks up
+ * the array's device address and should come before any stream capture.  All
+ * calls share the array: calls whose kernels overlap on the GPU race and give
+ * wrong results.  Failures are reported like those of the other entry points
+ * (status and satgb_last_error_string); device-side wait timeouts are not. */
 satgb_status satgb_sat_noalloc(const satgb_sat_desc* desc, satgb_stream stream);
 
 /* ------------------------------------------------------------------------- */
@@ -261,7 +265,10 @@ satgb_status satgb_set_config(int config);
 /* ------------------------------------------------------------------------- */
 
 /* Synchronises `stream`, then reports (and clears) a device-side error of the
- * last calls on it: SATGB_ERR_TIMEOUT when a look-back wait gave up. */
+ * calls on it since the last check: SATGB_ERR_TIMEOUT when a look-back wait
+ * gave up (the results of that call are then incomplete).  A timed-out call
+ * does not affect the calls after it: each launch starts with a clear error
+ * word, and only the report waits here until it is read. */
 satgb_status satgb_stream_check(satgb_stream stream);
 
 /* Message for the last failing call on this host thread ("" when none). */

@@ -33,7 +33,11 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 LIB_PATH = os.path.join(BUILD_DIR, "liboracle.so")
 REF_LIB_PATH = os.path.join(REF_DIR, "libref_sat.so")
-DEFAULT_REFERENCE_SRC = "/root/reference/integralImage"
+# The reference checkout's integralImage/ directory, where one is present,
+# is named by the SATGB_REF_DIR environment variable (no default): without it
+# only the restatement is built, and the tests that need the reference's own
+# code skip.
+REF_DIR_ENV = "SATGB_REF_DIR"
 
 # dtype-pair name -> (numpy in dtype, numpy out dtype)
 PAIRS = {
@@ -67,13 +71,17 @@ def pair_name(in_dtype, out_dtype) -> str:
 
 def build(with_ref: Optional[bool] = None, quiet: bool = True) -> None:
     """Compile liboracle.so; also the reference's own CPU code into _ref/ when
-    the reference checkout is present (``with_ref=None`` means "if present")."""
+    SATGB_REF_DIR names the reference checkout (``with_ref=None`` means "if
+    it does")."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE, "all"], stdout=out)
-    ref_src = os.environ.get("SATGB_REFERENCE_SRC", DEFAULT_REFERENCE_SRC)
+    ref_src = os.environ.get(REF_DIR_ENV, "")
+    present = bool(ref_src) and os.path.isfile(os.path.join(ref_src, "integralImage.h"))
     if with_ref is None:
-        with_ref = os.path.isfile(os.path.join(ref_src, "integralImage.h"))
+        with_ref = present
     if with_ref:
+        if not present:
+            raise RuntimeError(f"{REF_DIR_ENV} must name the reference's integralImage/ directory")
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_src}"],
                               stdout=out, stderr=subprocess.DEVNULL if quiet else None)
 

@@ -71,7 +71,7 @@ __device__ __forceinline__ Win win(int i, int r, int n, float inv_full) {
 // largest radius and so for all: then the four corners sit at fixed offsets and
 // a thread issues all its rows' corner loads before it needs them.
 __device__ __forceinline__ bool fwd_block_interior(const BoxArgs& a, int x0, int y0) {
-  const int W = (int)a.w, H = (int)a.h, r = a.rmax;
+  const long long W = a.w, H = a.h, r = a.rmax;
   return x0 - r - 1 >= 0 && x0 + kBX - 1 + r <= W - 1 && y0 - r - 1 >= 0 && y0 + kBY * kRows - 1 + r <= H - 1;
 }
 
@@ -214,7 +214,7 @@ __device__ __noinline__ float adjoint_edge_warp(const float* g, long long pitch,
 // corner at each of its positions have whole windows, for every radius: then
 // the taps sit at fixed offsets (and the block misses the last row and column).
 __device__ __forceinline__ bool bwd_block_interior(const BoxArgs& a, int x0, int y0) {
-  const int W = (int)a.w, H = (int)a.h, r2 = 2 * a.rmax;
+  const long long W = a.w, H = a.h, r2 = 2LL * a.rmax;
   return x0 >= r2 && x0 + kBX - 1 <= W - 2 - r2 && y0 >= r2 && y0 + kBY * kBRows - 1 <= H - 2 - r2;
 }
 
@@ -366,12 +366,16 @@ satgb_status check_desc_(const satgb_box_desc* d, BoxArgs& a) {
     a.inv_full[i] = 1.0f;
     a.box[i] = nullptr;
   }
+  // A window of radius max(W, H) - 1 around any pixel already covers the whole
+  // image, so larger radii give the same means: they are clamped there, which
+  // keeps every index expression of the kernels (x + r, 2r + 1, ...) in int.
+  const int64_t rcap = (d->width > d->height ? d->width : d->height) - 1;
   for (int i = 0; i < d->n_radii; ++i) {
     if (d->radius[i] < 0 || !d->d_box[i]) return SATGB_ERR_INVALID_ARG;
     if (((uintptr_t)d->d_box[i] % 4) != 0) return SATGB_ERR_MISALIGNED;
-    a.r[i] = d->radius[i];
+    a.r[i] = (int)((int64_t)d->radius[i] < rcap ? (int64_t)d->radius[i] : rcap);
     a.rmax = a.r[i] > a.rmax ? a.r[i] : a.rmax;
-    a.inv_full[i] = 1.0f / (float)(2 * (double)d->radius[i] + 1);
+    a.inv_full[i] = 1.0f / (float)(2 * (double)a.r[i] + 1);
     a.box[i] = static_cast<float*>(d->d_box[i]);
   }
   return SATGB_OK;

@@ -303,6 +303,31 @@ __device__ __forceinline__ void record_error(const SatParams& P, long long tile)
   if (atomicCAS(&P.ws->error, 0u, kDevErrTimeout) == 0u) P.ws->error_tile = (uint32_t)tile;
 }
 
+// End of a launch, called by thread 0 of every CTA after its last tile: the
+// last CTA to get here resets the ticket and the CTA count, moves a recorded
+// error to the sticky word (and clears it for the next launch) and advances
+// the epoch, which invalidates every status word of this launch.
+__device__ __forceinline__ void finish_launch(const SatParams& P, uint32_t epoch) {
+  __threadfence();
+  const uint32_t prev = atomicAdd(&P.ws->done, 1u);
+  if (prev == gridDim.x - 1) {
+    __threadfence();
+    const uint32_t err = ld_relaxed_u32(&P.ws->error);
+    if (err != 0u) {
+      if (P.ws->sticky == 0u) {
+        P.ws->sticky = err;
+        P.ws->sticky_tile = P.ws->error_tile;
+      }
+      P.ws->error = 0u;
+      P.ws->error_tile = 0u;
+    }
+    P.ws->ticket = 0ull;
+    P.ws->done = 0u;
+    P.ws->epoch = epoch + 1u;
+    __threadfence();
+  }
+}
+
 // Bounded wait for an mbarrier phase; false (and an error recorded) when the
 // wait limit runs out.
 static __device__ __noinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, const SatParams& P, long long tile) {
@@ -1075,17 +1100,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
 
   // ---- end of launch: the last CTA resets the ticket and advances the epoch --
   __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    const uint32_t prev = atomicAdd(&P.ws->done, 1u);
-    if (prev == gridDim.x - 1) {
-      __threadfence();
-      P.ws->ticket = 0ull;
-      P.ws->done = 0u;
-      P.ws->epoch = epoch + 1u;
-      __threadfence();
-    }
-  }
+  if (tid == 0) finish_launch(P, epoch);
 }
 
 }  // namespace satgb

@@ -477,17 +477,7 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
 
   // ---- end of launch: the last CTA resets the ticket and advances the epoch --
   __syncthreads();
-  if (tid == 0) {
-    __threadfence();
-    const uint32_t prev = atomicAdd(&P.ws->done, 1u);
-    if (prev == gridDim.x - 1) {
-      __threadfence();
-      P.ws->ticket = 0ull;
-      P.ws->done = 0u;
-      P.ws->epoch = epoch + 1u;
-      __threadfence();
-    }
-  }
+  if (tid == 0) finish_launch(P, epoch);
 }
 
 }  // namespace satgb

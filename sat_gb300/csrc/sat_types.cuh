@@ -195,13 +195,19 @@ __device__ __forceinline__ void publish(unsigned long long* words, A val, uint32
 }
 
 // Workspace header (device memory, zero-initialised once at allocation).
+// `error` belongs to the running launch: once set, every bounded wait of that
+// launch gives up at once, so the launch ends quickly.  The last CTA of the
+// launch moves it to `sticky` (kept until the host reads and clears it) and
+// resets it, so one timed-out launch never cuts short the waits of the next.
 struct WsHeader {
   unsigned long long ticket; // next tile ticket of the running launch
   uint32_t done;             // CTAs that finished the running launch
   uint32_t epoch;            // launch counter; advanced by the last CTA of each launch
-  uint32_t error;            // 0, or a device error code (kDevErrTimeout)
-  uint32_t error_tile;       // tile that recorded the error
-  uint32_t pad[10];
+  uint32_t error;            // 0, or a device error code (kDevErrTimeout) of the running launch
+  uint32_t error_tile;       // tile that recorded it
+  uint32_t sticky;           // the first error of the launches since the host last cleared it
+  uint32_t sticky_tile;      // tile that recorded it
+  uint32_t pad[8];
 };
 static_assert(sizeof(WsHeader) == 64, "header is one 64-byte block");
 

@@ -354,6 +354,59 @@ satgb_status validate_image(const ImgCheck& c, size_t in_sz, size_t out_sz) {
   return SATGB_OK;
 }
 
+// The images of one batch run concurrently in one launch, so no image may
+// write memory another image reads or writes.  Inputs may be shared (they are
+// only read); an image computed in place is one output range.  Ranges are the
+// byte extents from the first to the last element; two ranges of images with
+// the same row pitch whose rows fall into disjoint columns of that pitch (side
+// by side in one pitched buffer) do not touch each other and pass.  Sorting by
+// start and keeping the open ranges makes the check O(n log n) unless many
+// ranges overlap (then it compares each new range with every open one).
+struct ByteRange {
+  uintptr_t b, e; // [b, e)
+  uint64_t pitch, row;
+  size_t img;
+  bool out;
+};
+
+bool ranges_touch(const ByteRange& x, const ByteRange& y) {
+  if (x.e <= y.b || y.e <= x.b) return false;
+  if (x.pitch != y.pitch || x.pitch == 0) return true;
+  // same pitch: the columns of each modulo the pitch, on a circle of length pitch
+  const uint64_t P = x.pitch;
+  const uint64_t a = ((uint64_t)(y.b % P) + P - (uint64_t)(x.b % P)) % P; // y's start relative to x's
+  return a < x.row || a + y.row > P;
+}
+
+satgb_status check_batch_disjoint(const std::vector<ImgCheck>& imgs, size_t in_sz, size_t out_sz) {
+  std::vector<ByteRange> r;
+  r.reserve(2 * imgs.size());
+  for (size_t i = 0; i < imgs.size(); ++i) {
+    const ImgCheck& c = imgs[i];
+    const uintptr_t ib = (uintptr_t)c.in, ob = (uintptr_t)c.out;
+    const uintptr_t ie = ib + (uintptr_t)(((c.height - 1) * c.in_pitch + c.width) * (long long)in_sz);
+    const uintptr_t oe = ob + (uintptr_t)(((c.height - 1) * c.out_pitch + c.width) * (long long)out_sz);
+    const bool same = ib == ob && in_sz == out_sz && c.in_pitch == c.out_pitch;
+    const uint64_t ip = c.height > 1 ? (uint64_t)c.in_pitch * in_sz : 0, op = c.height > 1 ? (uint64_t)c.out_pitch * out_sz : 0;
+    if (!same) r.push_back({ib, ie, ip, (uint64_t)c.width * in_sz, i, false});
+    r.push_back({ob, oe, op, (uint64_t)c.width * out_sz, i, true});
+  }
+  std::sort(r.begin(), r.end(), [](const ByteRange& x, const ByteRange& y) { return x.b < y.b; });
+  std::vector<const ByteRange*> open;
+  for (const ByteRange& x : r) {
+    size_t k = 0;
+    for (size_t j = 0; j < open.size(); ++j)
+      if (open[j]->e > x.b) open[k++] = open[j];
+    open.resize(k);
+    for (const ByteRange* y : open)
+      if ((x.out || y->out) && x.img != y->img && ranges_touch(*y, x))
+        return fail(SATGB_ERR_INVALID_ARG, "images %zu and %zu of the batch overlap (one writes memory the other uses)",
+                    std::min(x.img, y->img), std::max(x.img, y->img));
+    open.push_back(&x);
+  }
+  return SATGB_OK;
+}
+
 // ----------------------------------------------------------------------------
 // tuning table: (in, out, mode, dir, log2 w bucket, log2 h bucket, SMs) -> cfg
 // ----------------------------------------------------------------------------
@@ -706,10 +759,10 @@ satgb_status satgb_stream_check(satgb_stream stream) {
       cudaGetLastError();
       return;
     }
-    if (h.error != 0) {
-      result = fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.error_tile);
+    if (h.sticky != 0) {
+      result = fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.sticky_tile);
       const uint32_t zero[2] = {0u, 0u};
-      cudaMemcpy((char*)ws.base + offsetof(WsHeader, error), zero, sizeof zero, cudaMemcpyHostToDevice);
+      cudaMemcpy((char*)ws.base + offsetof(WsHeader, sticky), zero, sizeof zero, cudaMemcpyHostToDevice);
     }
   };
   for (auto& kv : g_ws)
@@ -805,6 +858,10 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
       max_h = std::max(max_h, c.height);
       sum_px += (double)c.width * (double)c.height;
     }
+  }
+  {
+    satgb_status st = check_batch_disjoint(keep, in_sz, out_sz);
+    if (st != SATGB_OK) return st;
   }
   std::lock_guard<std::mutex> lk(g_mu);
   int dev = 0;
@@ -921,10 +978,10 @@ satgb_status satgb_batch_plan_check(satgb_batch_plan* p, satgb_stream stream) {
   WsHeader h;
   e = cudaMemcpy(&h, p->ws.base, sizeof h, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy");
-  if (h.error) {
+  if (h.sticky) {
     const uint32_t zero[2] = {0u, 0u};
-    cudaMemcpy((char*)p->ws.base + offsetof(WsHeader, error), zero, sizeof zero, cudaMemcpyHostToDevice);
-    return fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.error_tile);
+    cudaMemcpy((char*)p->ws.base + offsetof(WsHeader, sticky), zero, sizeof zero, cudaMemcpyHostToDevice);
+    return fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out (tile %u)", h.sticky_tile);
   }
   return SATGB_OK;
 }

@@ -22,15 +22,17 @@
 // All calls share the one array: calls whose kernels overlap on the GPU (on
 // different streams, or from different host threads) race on it and give
 // wrong results.  The array keeps the last call's contents; before each launch
-// the ticket, CTA count and error word are cleared with cudaMemsetAsync (not
-// an allocation), while the epoch and status words are kept on purpose: the
-// kernel tags every status word with the launch epoch, so old contents never
-// read as valid.
+// the ticket, CTA count and the running launch's error word are cleared with
+// cudaMemsetAsync (not an allocation), while the epoch and status words are
+// kept on purpose: the kernel tags every status word with the launch epoch,
+// so old contents never read as valid.
 //
-// A look-back wait that gives up records an error in the array's header, but
-// this entry point cannot report it without a synchronising read; callers
-// that need device-side error reporting use satgb_sat_ex with
-// satgb_stream_check.
+// Argument and CUDA failures are reported like those of every other entry
+// point (a status, and the message in satgb_last_error_string), and each
+// launch is counted by satgb_launch_count.  A look-back wait that gives up
+// records an error in the array's header, but this entry point cannot report
+// it without a synchronising read; callers that need device-side error
+// reporting use satgb_sat_ex with satgb_stream_check.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -44,6 +46,11 @@
 #include "sat_kernel.cuh"
 #include "sat_registry.h"
 
+namespace satgb {
+satgb_status api_fail(satgb_status st, const char* msg);
+void api_count_launch();
+}  // namespace satgb
+
 namespace {
 
 constexpr size_t kSatgbNoallocBytes = 16u << 20; // 16 MiB
@@ -55,12 +62,11 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kSatgbNoallocBy
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kMaxDevices] = {};
 int g_noalloc_grid_sms[kMaxDevices] = {};
-thread_local std::string g_noalloc_err;
 
+// Failures go to the library's error channel (satgb_last_error_string), like
+// those of every other entry point.
 satgb_status noalloc_fail(satgb_status st, const std::string& msg) {
-  g_noalloc_err = msg;
-  std::fprintf(stderr, "satgb_sat_noalloc: %s\n", msg.c_str());
-  return st;
+  return satgb::api_fail(st, ("satgb_sat_noalloc: " + msg).c_str());
 }
 
 size_t elem_size(int t) {
@@ -120,15 +126,17 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
   if (ntx > INT32_MAX || nty > INT32_MAX || need > kSatgbNoallocBytes) {
     char buf[256];
     std::snprintf(buf, sizeof buf,
-                  "a %lld x %lld image needs %zu bytes of look-back scratch; the fixed no-alloc array holds %zu",
+                  "a %lld x %lld image needs %zu bytes of look-back scratch; the fixed scratch array holds %zu",
                   (long long)d->width, (long long)d->height, need, kSatgbNoallocBytes);
     return noalloc_fail(SATGB_ERR_INVALID_ARG, buf);
   }
 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-    return noalloc_fail(SATGB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices)
+    return noalloc_fail(SATGB_ERR_CUDA, "device ordinal " + std::to_string(dev) + " is beyond the " +
+                                            std::to_string(kMaxDevices) + " devices this entry point keeps scratch addresses for");
   void* base = nullptr;
   int sms = 0;
   {
@@ -179,5 +187,6 @@ extern "C" satgb_status satgb_sat_noalloc(const satgb_sat_desc* d, satgb_stream 
   P.stall_tile = -1;
   e = v->launch(P, grid, s);
   if (e != cudaSuccess) return noalloc_fail(SATGB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+  satgb::api_count_launch();
   return SATGB_OK;
 }

@@ -13,7 +13,8 @@ Small cases store input and output arrays; the 1024x1024 cases (the
 reference's own smallest benchmark size, ScanRow-BRLT.cu:272-273) store the
 generator spec plus SHA-256 digests of input and output.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root, with SATGB_REF_DIR naming the reference checkout's
+integralImage/ directory:  SATGB_REF_DIR=<checkout>/integralImage python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -9,7 +9,8 @@ oracle/_ref/libref_sat.so.
 The fixtures pin the oracle's scans (tests/test_oracle.py) and the CUDA scans
 (tests/test_gpu_parity.py) on machines where the reference is absent.
 
-Run from the repository root:  python tests/golden/make_golden_scans.py
+Run from the repository root, with SATGB_REF_DIR naming the reference checkout's
+integralImage/ directory:  SATGB_REF_DIR=<checkout>/integralImage python tests/golden/make_golden_scans.py
 """
 from __future__ import annotations
 

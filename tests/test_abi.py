@@ -152,6 +152,36 @@ def test_batch_plan_validation(satlib):
     assert satlib.satgb_batch_plan_destroy(None) == _lib.OK
 
 
+def test_batch_plan_rejects_images_that_overlap(satlib):
+    """The images of a batch run at once, so no image may write memory that
+    another image reads or writes; shared inputs and images side by side in
+    one pitched buffer are fine.  The check runs before any device call."""
+    def create(*images):
+        arr = (_lib.satgb_image * len(images))()
+        for i, im in enumerate(images):
+            arr[i] = _lib.satgb_image(*im)
+        plan = ctypes.c_void_p()
+        st = satlib.satgb_batch_plan_create(ctypes.byref(plan), _lib.U8, _lib.U32, 0, 0, arr, len(images), None)
+        if st == _lib.OK:  # with a GPU: the plan captured its launch but never ran it
+            satlib.satgb_batch_plan_destroy(plan)
+        return st
+
+    def overlap(st):
+        return st == _lib.ERR_INVALID_ARG and b"overlap" in satlib.satgb_last_error_string()
+
+    # (d_in, in_pitch, d_out, out_pitch, width, height); u8 inputs, u32 outputs
+    a = (0x100000, 64, 0x800000, 64, 64, 64)
+    assert overlap(create(a, (0x200000, 64, 0x800000 + 4 * 64 * 10, 64, 64, 64)))  # outputs overlap
+    assert overlap(create(a, (0x800000 + 100, 64, 0x900000, 64, 64, 64)))         # reads image 0's output
+    assert overlap(create(a, (0x200000, 64, 0x100000, 16, 16, 16)))               # writes image 0's input
+    assert not overlap(create(a, (0x100000, 64, 0x900000, 64, 64, 64)))           # shared input
+    # side by side in one pitched buffer (pitch 128 elements): columns 0-63 and 64-127
+    b = (0x100000, 128, 0x800000, 128, 64, 64)
+    c = (0x100000 + 64, 128, 0x800000 + 4 * 64, 128, 64, 64)
+    assert not overlap(create(b, c))
+    assert overlap(create(b, (0x100000 + 32, 128, 0x800000 + 4 * 32, 128, 64, 64)))  # columns 32-95
+
+
 def test_python_api_rejects_cpu_tensors(satlib):
     torch = pytest.importorskip("torch")
     import sat_gb300

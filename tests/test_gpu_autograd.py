@@ -118,6 +118,70 @@ def test_box_means_forward(cuda, shape):
         assert err <= tol, (r, err, tol)
 
 
+def _four_corner64(S: torch.Tensor, radii):
+    """Box means in float64 from the given SAT S (..., H, W) by the four-corner
+    rule, and per element the magnitudes |A| + |B| of its two row-segment
+    differences A = S(yb,xb) - S(yb,xa-1), B = S(ya-1,xb) - S(ya-1,xa-1)."""
+    H, W = S.shape[-2:]
+    P = torch.nn.functional.pad(S.double(), (1, 0, 1, 0))
+    ys = torch.arange(H, device=S.device)
+    xs = torch.arange(W, device=S.device)
+    means, mags = [], []
+    for r in radii:
+        ya, yb = (ys - r).clamp(min=0), (ys + r).clamp(max=H - 1)
+        xa, xb = (xs - r).clamp(min=0), (xs + r).clamp(max=W - 1)
+        A = P[..., yb + 1, :][..., xb + 1] - P[..., yb + 1, :][..., xa]
+        B = P[..., ya, :][..., xb + 1] - P[..., ya, :][..., xa]
+        area = ((yb - ya + 1).double()[:, None] * (xb - xa + 1).double()[None, :])
+        means.append((A - B) / area)
+        mags.append((A.abs() + B.abs()) / area)
+    return torch.stack(means, dim=-3), torch.stack(mags, dim=-3)
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 256, 256), (1, 1, 1024, 1024)])
+def test_box_means_forward_interior_blocks(cuda, shape):
+    """Sizes where most blocks of the forward kernel are interior (every
+    output of the 32 x 64 block has the whole window of the largest radius and
+    the row and column before it), so the branch-free path is what is checked.
+    Each mean is compared with the four-corner rule evaluated in float64 on the
+    kernel's own f32 SAT: the kernel does two f32 subtractions of corner
+    values, one of the differences and a multiply by the f32 1/area^2, so
+    |m - m64| <= 2 eps32 (|A| + |B|) / area + 4 eps32 |m64| per element.  The
+    means are also checked end to end against float64 from x with the file's
+    tolerance."""
+    g = torch.Generator(device="cpu").manual_seed(31)
+    x = torch.randn(shape, generator=g, dtype=torch.float32).to(cuda)
+    radii = (3, 7, 15)
+    S = sat_gb300.sat(x, torch.float32)
+    m = api.box_means_from_sat(S, radii)
+    m64, mag = _four_corner64(S, radii)
+    err = (m.double() - m64).abs()
+    bound = 2 * EPS32 * mag + 4 * EPS32 * m64.abs() + 1e-30
+    assert bool((err <= bound).all()), float((err / bound).max())
+    # the interior fraction really is the bulk: blocks of 32 columns x 64 rows
+    H, W = shape[-2:]
+    rmax = max(radii)
+    bx = [x0 for x0 in range(0, W, 32) if x0 - rmax - 1 >= 0 and x0 + 31 + rmax <= W - 1]
+    by = [y0 for y0 in range(0, H, 64) if y0 - rmax - 1 >= 0 and y0 + 63 + rmax <= H - 1]
+    assert len(bx) * len(by) >= 0.5 * (-(-W // 32)) * (-(-H // 64))
+    ref = box_means64(x, radii)
+    smax = float(sat64(x.abs()).max())
+    for k, r in enumerate(radii):
+        tol = 4 * EPS32 * smax / (r + 1) ** 2 + 1e-7
+        assert float((m[..., k, :, :].double() - ref[..., k, :, :]).abs().max()) <= tol, r
+
+
+def test_box_means_huge_radius_is_the_whole_image(cuda):
+    """A radius far beyond the image (up to INT_MAX) filters like radius
+    max(H, W) - 1, whose window already covers the whole image."""
+    x = torch.rand((2, 33, 70), device=cuda)
+    S = sat_gb300.sat(x, torch.float32)
+    m = api.box_means_from_sat(S, (69, 1 << 20, 2**31 - 1))
+    full = x.double().mean(dim=(-2, -1))[:, None, None, None].expand(2, 3, 33, 70)
+    assert torch.allclose(m.double(), full, atol=1e-5)
+    assert torch.equal(m[:, 0], m[:, 1]) and torch.equal(m[:, 0], m[:, 2])
+
+
 def test_box_means_single_radius_matches_full_sum(cuda):
     x = torch.rand((3, 17, 29), device=cuda)
     m = AG.box_filter_means(x, (100,))
@@ -147,9 +211,9 @@ def test_box_grad_vs_float64_cumsum(cuda, shape):
 
 
 @pytest.mark.parametrize("shape,radii", [
-    ((1, 2, 200, 333), (2, 9, 32)),   # staged tiles, the largest staged radius, ragged tiles
-    ((1, 1, 130, 170), (33,)),        # above the staged limit: the per-tap gather
-    ((1, 1, 97, 131), (0, 1, 32, 70)),  # staged radii next to one past every side
+    ((1, 2, 200, 333), (2, 9, 32)),   # interior blocks next to border blocks, ragged block edges
+    ((1, 1, 130, 170), (33,)),        # a radius whose window spans most of the image: no interior block
+    ((1, 1, 97, 131), (0, 1, 32, 70)),  # radius 0, and a radius wider than the image on one side
 ])
 def test_box_grad_tiles_and_large_radii(cuda, shape, radii):
     g = torch.Generator(device="cpu").manual_seed(25)

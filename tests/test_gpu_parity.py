@@ -89,7 +89,7 @@ SHAPES = [(1, 1), (1, 700), (700, 1), (2, 3), (63, 127), (64, 128), (65, 129), (
           (129, 257), (300, 1000), (1000, 300), (517, 769)]
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 4])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_all_pairs_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -103,7 +103,7 @@ def test_all_pairs_all_configs(cuda, oracle, cfg):
         sat_gb300.set_config(-1)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 4])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_reverse_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -223,6 +223,24 @@ def test_compensated_f32(cuda, oracle, kind):
     rc = to_np(sat_gb300.sat(x, torch.float32, mode="compensated", reverse=True))
     e_rev = oracle.err_stats(rc, oracle.sat_fp64(a, reverse=True), oracle.sat_fp64(a, reverse=True, absval=True))
     assert e_rev["max_rel_abs"] <= TOL_COMP, e_rev
+
+
+@pytest.mark.parametrize("kind", ["f32u", "f32log"])
+def test_compensated_register_tiles_forward_and_reverse(cuda, oracle, kind):
+    """Configuration 3 (the register-resident 128-row tiles, the default for
+    large compensated images) forced on every edge shape and at 2048^2,
+    forward and reverse: the reverse compensated SAT is the backward of the
+    compensated autograd SAT."""
+    sat_gb300.set_config(3)
+    try:
+        for i, shape in enumerate(SHAPES + [(2048, 2048)]):
+            a = oracle.gen(kind, 6000 + i, shape)
+            x = to_dev(a)
+            for rev in (False, True):
+                out = to_np(sat_gb300.sat(x, torch.float32, mode="compensated", reverse=rev))
+                _check_float(oracle, a, out, TOL_COMP, reverse=rev)
+    finally:
+        sat_gb300.set_config(-1)
 
 
 def test_compensated_u8_and_i8_inputs(cuda, oracle):
@@ -376,23 +394,36 @@ def test_full_size_8192_u8_u32_bit_exact(cuda, oracle):
         assert np.array_equal(out, oracle.sat_serial(a, np.uint32)), fn.__name__
 
 
+def _precision_8192(oracle, kind):
+    a = oracle.gen(kind, 8193, (8192, 8192))
+    x = to_dev(a)
+    ref = oracle.sat_fp64(a)
+    den = oracle.sat_fp64(a, absval=True)
+    e_plain = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32)), ref, den)
+    e_comp = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32, mode="compensated")), ref, den)
+    print(f"\n[precision 8192^2 {kind}] plain {e_plain}  compensated {e_comp}")
+    assert e_plain["max_rel_abs"] <= 1e-5, (kind, e_plain)
+    return e_plain, e_comp
+
+
 @pytest.mark.slow
-def test_full_size_8192_f32_precision(cuda, oracle):
-    """Both f32 input classes at 8192^2 (U[0,1), and magnitudes 10^U(-3,3) with
-    random signs): plain and compensated against the FP64 oracle.  The
-    measured errors are printed (pytest -s) for the record."""
-    for kind in ("f32u", "f32log"):
-        a = oracle.gen(kind, 8193, (8192, 8192))
-        x = to_dev(a)
-        ref = oracle.sat_fp64(a)
-        den = oracle.sat_fp64(a, absval=True)
-        e_plain = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32)), ref, den)
-        e_comp = oracle.err_stats(to_np(sat_gb300.sat(x, torch.float32, mode="compensated")), ref, den)
-        print(f"\n[precision 8192^2 {kind}] plain {e_plain}  compensated {e_comp}")
-        assert e_plain["max_rel_abs"] <= 1e-5, (kind, e_plain)
-        assert e_comp["max_rel_abs"] <= TOL_COMP, (kind, e_comp)
-        if kind == "f32u":
-            assert e_comp["max_rel"] <= 1e-6, e_comp
+def test_compensated_8192_uniform_within_1e6_relative(cuda, oracle):
+    """U[0,1) inputs at 8192^2: every compensated SAT element is within 1e-6
+    of the FP64 SAT relative to the element itself, |S - S64| / |S64|."""
+    _, e_comp = _precision_8192(oracle, "f32u")
+    assert e_comp["max_rel"] <= 1e-6, e_comp
+    assert e_comp["max_rel_abs"] <= TOL_COMP, e_comp
+
+
+@pytest.mark.slow
+def test_compensated_8192_log_class_relative_to_sat_of_abs(cuda, oracle):
+    """Magnitudes 10^U(-3,3) with random signs at 8192^2: sums cancel, so some
+    exact elements are near 0 and no fixed-precision sum bounds the error
+    relative to the element itself.  The stated bound for this class uses the
+    condition-aware denominator SAT(|a|): |S - S64| / SAT(|a|)64 <= 2e-7
+    (measured: about 3e-8); the relative error on elements is reported."""
+    _, e_comp = _precision_8192(oracle, "f32log")
+    assert e_comp["max_rel_abs"] <= TOL_COMP, e_comp
 
 
 @pytest.mark.slow
@@ -522,3 +553,48 @@ def test_scans_pitched_and_full_size(cuda, oracle):
     assert int(r[:, -1].view(torch.int32).to(torch.int64).remainder(1 << 32).sum().item()) % (1 << 32) == total
     assert int(c[-1, :].view(torch.int32).to(torch.int64).remainder(1 << 32).sum().item()) % (1 << 32) == total
     assert int(s[-1, -1].view(torch.int32).to(torch.int64).item()) % (1 << 32) == total
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("pitched", [True, False])
+def test_batch512_bit_exact(cuda, oracle, pitched):
+    """The batch workload exactly as the bench builds it: 512 u8 images with
+    widths and heights log-uniform in [64, 4096] (about 590 M pixels, 78,000
+    tiles), rows pitched to 128 bytes or packed, one graph replay of the plan;
+    every image bit-exact against the oracle."""
+    from bench import build_batch
+    xs, ys, _ = build_batch(cuda, pitched=pitched)
+    plan = sat_gb300.BatchPlan(xs, ys)
+    for y in ys:
+        y.view(torch.int32).fill_(-1)
+    plan.exec()
+    plan.check()
+    for i, (x, y) in enumerate(zip(xs, ys)):
+        a = to_np(x)
+        assert np.array_equal(bits(to_np(y)), bits(oracle.sat_serial(a, np.uint32))), i
+    plan.close()
+
+
+@pytest.mark.slow
+def test_stress_32768_u8_u32_bit_exact(cuda, oracle):
+    """32768 x 32768 u8 -> u32 (2^30 pixels; sums wrap mod 2^32 many times)
+    bit-exact against the oracle."""
+    a = oracle.gen("u8", 32768, (32768, 32768))
+    x = to_dev(a)
+    out = sat_gb300.sat(x, torch.uint32)
+    del x
+    got = to_np(out)
+    del out
+    assert np.array_equal(got, oracle.sat_serial(a, np.uint32))
+
+
+@pytest.mark.slow
+def test_stress_16384_compensated_f32(cuda, oracle):
+    """16384 x 16384 U[0,1) through the compensated f32 SAT: within 1e-6 of
+    the FP64 SAT relative to each element, and 2e-7 relative to SAT(|a|)."""
+    a = oracle.gen("f32u", 16384, (16384, 16384))
+    comp = to_np(sat_gb300.sat(to_dev(a), torch.float32, mode="compensated"))
+    e = oracle.err_stats(comp, oracle.sat_fp64(a), oracle.sat_fp64(a, absval=True))
+    print(f"\n[precision 16384^2 f32u compensated] {e}")
+    assert e["max_rel"] <= 1e-6, e
+    assert e["max_rel_abs"] <= TOL_COMP, e
