@@ -454,6 +454,62 @@ __device__ __forceinline__ A resolve(EarlyWin<A>& e, const unsigned long long* b
   }
 }
 
+// resolve() for N elements of one thread at once (a look-back thread that owns
+// several columns or rows of a tile): every round walks each open element's
+// window, then re-reads the windows of all elements still open together, so
+// their round trips overlap instead of following one another.  Element i's
+// status words start at base0 + i * elem_step.
+template <class A, int N>
+__device__ __forceinline__ void resolve_n(EarlyWin<A> (&e)[N], const unsigned long long* base0, long long elem_step,
+                                          long long stride, int steps, uint32_t tagA, uint32_t tagI,
+                                          const SatParams& P, long long tile, A (&acc)[N]) {
+  constexpr int W = EarlyWin<A>::W;
+  int idx[N];
+  uint32_t open = 0;
+#pragma unroll
+  for (int n = 0; n < N; ++n) {
+    acc[n] = Ar<A>::zero();
+    idx[n] = 0;
+    if (steps > 0) open |= 1u << n;
+  }
+  unsigned long long t0 = 0;
+  unsigned ns = 0;
+  for (uint32_t round = 0; open; ++round) {
+    bool progressed = false;
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      if (!(open & (1u << n))) continue;
+#pragma unroll
+      for (int q = 0; q < W; ++q) {
+        A val;
+        const uint32_t st = decode_word<A>(e[n].w[q], tagA, tagI, val);
+        if (!st) break;
+        acc[n] = Ar<A>::add(val, acc[n]);
+        ++idx[n];
+        progressed = true;
+        if (st == kStateInc || idx[n] >= steps) {
+          open &= ~(1u << n);
+          break;
+        }
+      }
+    }
+    if (!open) break;
+    if (!progressed) {
+      if (t0 == 0) t0 = global_timer_ns();
+      if (ns) __nanosleep(ns);
+      ns = ns ? (ns < 256 ? 2 * ns : ns) : 32;
+      if ((round & 7u) == 7u &&
+          ((long long)(global_timer_ns() - t0) > P.wait_limit_ns || ld_relaxed_u32(&P.ws->error) != 0u)) {
+        record_error(P, tile);
+        return;
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < N; ++n)
+      if (open & (1u << n)) early_read<A>(e[n], base0 + n * elem_step, stride, steps, idx[n]);
+  }
+}
+
 // The fields of an image descriptor a tile needs, in registers.  For a single
 // image they are read straight from the kernel parameter (constant bank);
 // only batched launches read the descriptor table in global memory.

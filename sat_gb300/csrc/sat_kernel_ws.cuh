@@ -372,13 +372,16 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
         }
         agg[i] = ac;
       }
+      // all of this lane's columns resolve together (their round trips overlap)
+      A above[COLS_PER_LANE];
+      resolve_n<A, COLS_PER_LANE>(win, P.col_words + ((unsigned long long)t * TW + lane) * K, 32LL * K, cstride,
+                                  csteps, tagA, tagI, P, t, above);
 #pragma unroll
       for (int i = 0; i < COLS_PER_LANE; ++i) {
         const int j = lane + 32 * i;
         unsigned long long* base = P.col_words + ((unsigned long long)t * TW + j) * K;
-        const A above = resolve<A>(win[i], base, cstride, csteps, tagA, tagI, P, t);
-        if (pub_col) publish<A>(base, AR::add(above, agg[i]), tagI);
-        s_colabove[kb][j] = above;
+        if (pub_col) publish<A>(base, AR::add(above[i], agg[i]), tagI);
+        s_colabove[kb][j] = above[i];
       }
       if (lane == 0) {
         const A c = resolve<A>(cwin, cbase, kstride, csteps, tagA, tagI, P, t);
@@ -422,11 +425,12 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
         agg[i] = s_rowagg[kb][y];
         if (pub_row) publish<A>(base, agg[i], tagA);
       }
+      resolve_n<A, ROWS_PER_LANE>(win, P.row_words + ((unsigned long long)t * TH + lane * ROWS_PER_LANE) * K, K,
+                                  rstride, rsteps, tagA, tagI, P, t, left);
 #pragma unroll
       for (int i = 0; i < ROWS_PER_LANE; ++i) {
         const int y = lane * ROWS_PER_LANE + i;
         unsigned long long* base = P.row_words + ((unsigned long long)t * TH + y) * K;
-        left[i] = resolve<A>(win[i], base, rstride, rsteps, tagA, tagI, P, t);
         if (pub_row) publish<A>(base, AR::add(left[i], agg[i]), tagI);
         s_rowleft[kb][y] = left[i];
       }

@@ -163,7 +163,8 @@ def test_box_means_forward_interior_blocks(cuda, shape):
     rmax = max(radii)
     bx = [x0 for x0 in range(0, W, 32) if x0 - rmax - 1 >= 0 and x0 + 31 + rmax <= W - 1]
     by = [y0 for y0 in range(0, H, 64) if y0 - rmax - 1 >= 0 and y0 + 63 + rmax <= H - 1]
-    assert len(bx) * len(by) >= 0.5 * (-(-W // 32)) * (-(-H // 64))
+    frac = len(bx) * len(by) / ((-(-W // 32)) * (-(-H // 64)))
+    assert frac >= (0.8 if H >= 1024 else 0.35), frac  # 420 of 512 blocks at 1024^2, 12 of 32 at 256^2
     ref = box_means64(x, radii)
     smax = float(sat64(x.abs()).max())
     for k, r in enumerate(radii):

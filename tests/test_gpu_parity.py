@@ -347,16 +347,21 @@ def test_timeout_is_reported_and_context_survives(cuda, oracle, cfg):
         assert L.satgb_debug_stall_tile(5) == 0
         with torch.cuda.stream(s):
             sat_gb300.scanrow_brlt(x, torch.uint32)
+        L.satgb_debug_stall_tile(-1)
+        # the next call, queued before anyone read the error, is unaffected
+        with torch.cuda.stream(s):
+            after = sat_gb300.scanrow_brlt(x, torch.uint32)
         with pytest.raises(sat_gb300.SatError) as ei:
             sat_gb300.stream_check(s)
         assert ei.value.status == _lib.ERR_TIMEOUT
+        assert np.array_equal(to_np(after), oracle.sat_serial(a, np.uint32))
     finally:
         L.satgb_debug_stall_tile(-1)
         sat_gb300.set_wait_limit_us(2_000_000)
         sat_gb300.set_config(-1)
     with torch.cuda.stream(s):
         out = sat_gb300.scanrow_brlt(x, torch.uint32)
-    sat_gb300.stream_check(s)
+    sat_gb300.stream_check(s)  # the report was cleared by the check above
     assert np.array_equal(to_np(out), oracle.sat_serial(a, np.uint32))
 
 
