@@ -319,9 +319,9 @@ def run_gpu(args):
         "warmup_launches": int(warm_launches),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "traffic": _traffic_from_profiles("f32_f32_8192"),
+                     "traffic": _traffic_from_profiles("f32_f32_8192_ws"),
                      "algorithmic_bytes_per_launch": step_bytes,
-                     "kernel": "satgb::sat_tile_kernel<float,float,float,fwd>"},
+                     "kernel": "satgb::sat_tile_kernel_ws<float,float,float,fwd> (128-row tiles, direct stores)"},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "sub_results": sub,
@@ -430,6 +430,13 @@ CASES = {
     "u8r_8192": ("uint8", "uint32", "plain", True, 8192, 8192),
     "f64_4096": ("float64", "float64", "plain", False, 4096, 4096),
     "f32r_8192": ("float32", "float32", "plain", True, 8192, 8192),
+    "f32_1024": ("float32", "float32", "plain", False, 1024, 1024),
+    "f32_2048": ("float32", "float32", "plain", False, 2048, 2048),
+    "f32_4096": ("float32", "float32", "plain", False, 4096, 4096),
+    "f32_16384": ("float32", "float32", "plain", False, 16384, 16384),
+    "u8_1024": ("uint8", "uint32", "plain", False, 1024, 1024),
+    "f32c_2048": ("float32", "float32", "compensated", False, 2048, 2048),
+    "f32c_16384": ("float32", "float32", "compensated", False, 16384, 16384),
     "f32t_8192": ("float32", "float32", "rows_transposed", False, 8192, 8192),
     "u8t_8192": ("uint8", "uint32", "rows_transposed", False, 8192, 8192),
 }

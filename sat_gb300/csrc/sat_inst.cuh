@@ -86,37 +86,37 @@ Variant make_variant_r(int in_t, int out_t, int mode, int cfg) {
 
 // The same three for sat_tile_kernel_ws (warp-specialized; NWC compute warps
 // plus three role warps, one CTA per SM).
-template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC, bool DIRECT = false, int CTAS = 1>
 cudaError_t prepare_impl_ws() {
-  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CTAS>;
   constexpr int kMaxDev = 64;
   static std::atomic<int> done[kMaxDev];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
-  e = cudaFuncSetAttribute(&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC>,
+  e = cudaFuncSetAttribute(&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
   if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
   return e;
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC, bool DIRECT = false, int CTAS = 1>
 cudaError_t launch_impl_ws(const SatParams& p, int grid, cudaStream_t s) {
-  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
-  cudaError_t e = prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC>();
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CTAS>;
+  cudaError_t e = prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS>();
   if (e != cudaSuccess) return e;
-  sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
   return cudaGetLastError();
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC, bool DIRECT = false, int CTAS = 1>
 Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
-  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CTAS>;
   return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
-                 &launch_impl_ws<TIn, TOut, A, REV, RPW, NWC>,
-                 &prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC>,
-                 (const void*)&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC>,
+                 &launch_impl_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS>,
+                 &prepare_impl_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS>,
+                 (const void*)&sat_tile_kernel_ws<TIn, TOut, A, REV, RPW, NWC, DIRECT, CTAS>,
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
@@ -140,6 +140,9 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
 //      the compensated f32 SAT measured 0.284 ms with 64-row and 0.217 ms with
 //      128-row tiles at 8192^2)
 //   4: (1-byte inputs, 4-byte sums only, SG_TALL) pipelined, 256-row tiles, direct stores
+//   5: warp-specialized with direct stores, 8 rows a compute warp: 128-row
+//      tiles and 16 compute warps for 4-byte accumulators (64-row tiles and 8
+//      compute warps for 8-byte ones)
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_WS_RPW(A) (sizeof(A) == 8 ? 8 : 4)  /* 64-row tiles either way: */
@@ -148,7 +151,8 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
   satgb::make_variant_ws<TIN, TOUT, A, REV, SG_WS_RPW(A), SG_WS_NWC(A)>(IT, OT, MODE, 0), \
       satgb::make_variant<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),    \
       satgb::make_variant<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 2),       \
-      satgb::make_variant_r<TIN, TOUT, A, REV, 8, 16, 1>(IT, OT, MODE, 3)
+      satgb::make_variant_r<TIN, TOUT, A, REV, 8, 16, 1>(IT, OT, MODE, 3),               \
+      satgb::make_variant_ws<TIN, TOUT, A, REV, 8, SG_WS_NWC(A), true>(IT, OT, MODE, 5)
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
   SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
 

@@ -1,103 +1,127 @@
 // sat_kernel_ws.cuh -- the warp-specialized tile loop.
 //
 // Same decomposition, tickets, status words and look-backs as sat_tile_kernel
-// (sat_kernel.cuh); the work of a tile is split between warps that never wait
-// on one another at a CTA-wide barrier:
+// (sat_kernel.cuh); the work of a tile is split between warp groups that never
+// wait on one another at a CTA-wide barrier:
 //
 //   NWC compute warps   the local phase of tile k+1 (partials, the lanes' row
 //                       prefix E in registers), then the output phase of
-//                       tile k from its TMA stage, results back into the stage
-//   column warp         column sums over the compute warps: the column
+//                       tile k from its TMA stage
+//   column group        TW / 32 warps, one column per thread: the column
 //                       aggregate out at once, the exclusive prefix over the
-//                       warps, the column look-back; lane 0 the corner look-back
-//   row warp            row aggregates out, the row look-back, the scan of
-//                       rowleft over the tile's rows and u = sum rowleft (the
-//                       corner aggregate of the tile below)
-//   store warp          one TMA tensor store per tile, and the refill of the
-//                       stage it has read with the tile S ahead; tickets
+//                       compute warps, the column look-back; thread 0 also
+//                       the corner look-back
+//   row group           TH / 32 warps, one row per thread: the row aggregate
+//                       out, the row look-back, the scan of rowleft over the
+//                       tile's rows and u = sum rowleft (the corner aggregate
+//                       of the tile below)
+//   store warp          tickets and stage refills; without DIRECT also one TMA
+//                       tensor store per tile
+//
+// Every look-back thread owns one element, so a tile's look-back costs one
+// round trip to L2 (plus waits for late predecessors) instead of one per
+// element a thread owns; the look-back threads read their first window as
+// soon as the tile's input has arrived, before its partials are ready.
+//
+// Results leave in one of two ways.  Without DIRECT they go back into the
+// tile's stage and one TMA store moves them out; the stage is refilled once
+// that store has read it.  With DIRECT each thread stores its 16-byte row
+// segments straight from registers, and the stage (input only) goes back to
+// the producer as soon as the output phase has read it: the refill is no longer
+// held up by the output phase and its store, so the TMA ring keeps the loads a
+// whole tile further ahead of the compute warps.
 //
 // Hand-offs: named barriers AGG[2] (compute warps arrive when a tile's
-// partials are in shared memory, the look-back warps wait) and CAR[2] (the
-// look-back warps arrive when a tile's carries are in shared memory, the
+// partials are in shared memory, the look-back groups wait) and CAR[2] (the
+// look-back groups arrive when a tile's carries are in shared memory, the
 // compute warps wait), two of each by tile parity: a barrier is used again two
 // tiles later, when every participant has provably passed its previous phase.
 // Per stage, an mbarrier "done" (each compute warp arrives when its rows of the
-// tile's results are in the stage, the store warp waits); the compute warps
-// may run up to S-1 tiles ahead of the store warp, which an mbarrier's phase
-// parity tolerates and a named barrier would not.
-// The look-back of tile k therefore runs while the compute warps finish tile
-// k-1 and compute tile k+1's partials, and the TMA ring runs S-1 tiles ahead
-// of the compute warps because a stage is refilled as soon as its store has
-// read it.
+// tile's results are in the stage -- with DIRECT, when it has read the stage --
+// and the store warp waits); the compute warps may run up to S-1 tiles ahead
+// of the store warp, which an mbarrier's phase parity tolerates and a named
+// barrier would not.
 //
-// Shared vectors written by the look-back warps for tile k live in buffers
-// indexed k & 1; the compute warps' partials likewise, so the look-back warps
-// may read tile k's while the compute warps write tile k+1's.
+// Shared vectors written by the look-back groups for tile k live in buffers
+// indexed k & 1; the compute warps' partials likewise.  A group starts on
+// tile k+1 only after every compute warp has arrived at AGG(k+1), i.e. has
+// finished its output phase of tile k-1, the last reader of buffer (k+1) & 1.
 #pragma once
 #include "sat_kernel.cuh"
 
 namespace satgb {
 
-template <class TIn, class TOut, class A, int RPW, int NWC>
+// DIRECT: results go from registers straight to global memory (16-byte
+// stores, one per thread and row), so a stage holds only the tile's input.
+// CTAS: CTAs per SM the shared memory is split between.
+template <class TIn, class TOut, class A, int RPW, int NWC, bool DIRECT = false, int CTAS = 1>
 struct TileShapeWS {
   static constexpr int CPT = 16 / (int)sizeof(TOut);
   static constexpr int TW = 32 * CPT;
   static constexpr int TH = NWC * RPW;
+  static constexpr int NCW = TW / 32;          // column-group warps
+  static constexpr int NRW = TH / 32;          // row-group warps
+  static constexpr int RP = RPW > 4 ? 4 : RPW; // rows per pass of the lanes' row transpose
   static constexpr int IN_BYTES = TH * TW * (int)sizeof(TIn);
-  static constexpr int STAGE_BYTES = TH * TW * (int)(sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
+  static constexpr int STAGE_BYTES =
+      TH * TW * (int)(DIRECT || sizeof(TIn) > sizeof(TOut) ? sizeof(TIn) : sizeof(TOut));
   static constexpr int STATIC_BYTES =
-      (NWC * RPW * 32 + 2 * NWC * TW + 2 * TH + 2 * TW + 2 * TH + 2 * NWC + 8) * (int)sizeof(A) + 512;
-  static constexpr int S = Stages<STAGE_BYTES, STATIC_BYTES, 1>::value;
+      (NWC * RP * 32 + 2 * NWC * TW + 2 * TH + 2 * TW + 2 * TH + 2 * NWC + 2 * NRW + 8) * (int)sizeof(A) + 512;
+  static constexpr int S = Stages<STAGE_BYTES, STATIC_BYTES, CTAS>::value;
   static constexpr int DYN_SMEM = S * STAGE_BYTES;
-  static constexpr int THREADS = (NWC + 3) * 32;
+  static constexpr int THREADS = (NWC + NCW + NRW + 1) * 32;
 };
 
 // named barrier ids (0 is __syncthreads)
 constexpr int kBarAgg0 = 1; // + (k & 1)
 constexpr int kBarCar0 = 3; // + (k & 1)
 constexpr int kBarWiden = 5;
+constexpr int kBarRows = 6; // the row group's scan across its warps
 
 __device__ __forceinline__ void named_arrive(int id, int nthreads) {
   asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
-__global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __grid_constant__ SatParams P) {
-  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC>;
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC, bool DIRECT = false, int CTAS = 1>
+__global__ void __launch_bounds__(TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CTAS>::THREADS, CTAS)
+    sat_tile_kernel_ws(const __grid_constant__ SatParams P) {
+  using SH = TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CTAS>;
   constexpr int CPT = SH::CPT;
   constexpr int TW = SH::TW;
   constexpr int TH = SH::TH;
   constexpr int S = SH::S;
+  constexpr int NCW = SH::NCW, NRW = SH::NRW;
   constexpr int STAGE_ELEMS = SH::STAGE_BYTES / (int)sizeof(TIn);
-  constexpr int WCOL = NWC, WROW = NWC + 1, WSTORE = NWC + 2; // warp roles
-  constexpr int NAGG = (NWC + 2) * 32;   // compute + look-back warps
-  constexpr int COLS_PER_LANE = TW / 32; // column warp: slots lane + 32 i
-  constexpr int ROWS_PER_LANE = TH / 32; // row warp: rows lane * ROWS_PER_LANE + i
-  static_assert(TW % 32 == 0 && TH % 32 == 0, "look-back warps hold whole lanes' worth");
-  static_assert(32 % RPW == 0, "rows per warp divide the warp");
+  constexpr int WCOL = NWC, WROW = NWC + NCW, WSTORE = NWC + NCW + NRW; // first warp of each role
+  constexpr int NAGG = (NWC + NCW + NRW) * 32;                           // compute + look-back warps
+  constexpr int RP = SH::RP;   // rows per transpose pass ...
+  constexpr int LPR = 32 / RP; // ... lanes per row ...
+  constexpr int CH = RP;       // ... and values per lane
+  static_assert(TW % 32 == 0 && TH % 32 == 0, "look-back groups are whole warps");
+  static_assert(RPW % RP == 0 && 32 % RP == 0, "whole transpose passes");
   static_assert(S >= 3, "stages for the tile in output, the one in the local phase and one loading");
-  constexpr int LPR = 32 / RPW; // transpose-scan: lanes per row ...
-  constexpr int CH = RPW;       // ... and values per lane
   constexpr int K = Ar<A>::K;
-  constexpr bool WIDEN = sizeof(TIn) < sizeof(TOut);
+  constexpr bool WIDEN = !DIRECT && sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
   using AR = Ar<A>;
 
   extern __shared__ __align__(128) unsigned char dsmem[];
   TIn* stages = reinterpret_cast<TIn*>(dsmem);
 
-  __shared__ A s_tr[NWC][RPW][32];   // compute warps: transpose scratch (lane ^ row: conflict free)
+  __shared__ A s_tr[NWC][RP][32];    // compute warps: transpose scratch (lane ^ row: conflict free)
   __shared__ A s_colp[2][NWC][TW];   // per tile parity and warp: column partials, then their exclusive prefix over the warps
   __shared__ A s_rowagg[2][TH];      // row totals
   __shared__ A s_colabove[2][TW];    // column look-back results (by slot)
   __shared__ A s_rowleft[2][TH];     // row look-back results
   __shared__ A s_rlprev[2][NWC];     // per compute warp: sum of rowleft over the rows before it (scan order)
+  __shared__ A s_rwt[2][NRW];        // row group: sum of rowleft over each warp's 32 rows
   __shared__ A s_corner[2], s_u[2];
   __shared__ int s_cnt_corner[2];    // arrivals of {corner, u} per tile parity
   __shared__ long long s_tile[S];    // spatial tile index per stage (-1: no more tiles)
   __shared__ int s_img[S];
   __shared__ int s_tx[S], s_ty[S], s_pl[S];
   __shared__ __align__(8) unsigned long long s_full[S];
-  __shared__ __align__(8) unsigned long long s_done[S]; // the stage's results are complete
+  // the stage's results are complete (DIRECT: the stage has been read and may be refilled)
+  __shared__ __align__(8) unsigned long long s_done[S];
 
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -129,7 +153,33 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
   }
   __syncthreads();
 
-  if (warp == WSTORE && lane == 0) {
+  if (DIRECT && warp == WSTORE && lane == 0) {
+    // ---- producer thread: each stage is refilled once the output phase of its
+    //      tile has read it --------------------------------------------------------
+    TilePlan next;
+    bool have_next = false;
+    if (producing) {
+      next = plan_tile<REV>(P, pending);
+      have_next = true;
+      if (next.t >= 0) pending = atomicAdd(&P.ws->ticket, 1ull);
+    }
+    for (int k = 0; have_next; ++k) {
+      // tile k is a real tile (the one S ahead of it is still to come): its
+      // output phase arrives on the stage's barrier
+      const int st = k % S;
+      mbar_wait_bounded(smem_u32(&s_done[st]), (k / S) & 1, P, -1);
+      issue_tile<TIn, TW, TH, SH::IN_BYTES>(P, next, st, stages + st * STAGE_ELEMS, s_tile, s_img, s_tx, s_ty, s_pl,
+                                           s_full);
+      have_next = false;
+      if (next.t >= 0) {
+        next = plan_tile<REV>(P, pending);
+        have_next = true;
+        if (next.t >= 0) pending = atomicAdd(&P.ws->ticket, 1ull);
+      }
+    }
+  }
+
+  if (!DIRECT && warp == WSTORE && lane == 0) {
     // ---- store thread: one store per tile, then the refill of its stage -------
     TilePlan next;
     bool have_next = false;
@@ -172,7 +222,7 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
     // ---- compute warps ----------------------------------------------------------
     A E_nxt[RPW], E_cur[RPW];
     // local phase of tile kk: false when the tickets ran out (the look-back
-    // warps still get their AGG arrival, to see the end)
+    // groups still get their AGG arrival, to see the end)
     auto local_phase = [&](int kk) -> bool {
       const int st = kk % S;
       mbar_wait_bounded(smem_u32(&s_full[st]), (kk / S) & 1, P, -1);
@@ -210,36 +260,40 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
         }
         rowp[r] = rs;
       }
-      // row partials -> exclusive prefix over the lanes (E) and the row totals
+      // row partials -> exclusive prefix over the lanes (E) and the row totals,
+      // RP rows per pass through the transpose scratch
 #pragma unroll
-      for (int r = 0; r < RPW; ++r) s_tr[warp][r][lane ^ r] = rowp[r];
-      __syncwarp();
-      {
-        const int r = lane / LPR, q = lane % LPR;
-        A tot = AR::zero();
+      for (int h = 0; h < RPW / RP; ++h) {
 #pragma unroll
-        for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][(q * CH + (REV ? CH - 1 - i : i)) ^ r]);
-        A incl = tot;
+        for (int r = 0; r < RP; ++r) s_tr[warp][r][lane ^ r] = rowp[h * RP + r];
+        __syncwarp();
+        {
+          const int r = lane / LPR, q = lane % LPR;
+          A tot = AR::zero();
 #pragma unroll
-        for (int d = 1; d < LPR; d <<= 1) {
-          const A o = REV ? AR::shfl_down(incl, d, LPR) : AR::shfl_up(incl, d, LPR);
-          if (REV ? (q + d < LPR) : (q >= d)) incl = AR::add(o, incl);
+          for (int i = 0; i < CH; ++i) tot = AR::add(tot, s_tr[warp][r][(q * CH + (REV ? CH - 1 - i : i)) ^ r]);
+          A incl = tot;
+#pragma unroll
+          for (int d = 1; d < LPR; d <<= 1) {
+            const A o = REV ? AR::shfl_down(incl, d, LPR) : AR::shfl_up(incl, d, LPR);
+            if (REV ? (q + d < LPR) : (q >= d)) incl = AR::add(o, incl);
+          }
+          A ex = REV ? AR::shfl_down(incl, 1, LPR) : AR::shfl_up(incl, 1, LPR);
+          if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
+#pragma unroll
+          for (int i = 0; i < CH; ++i) {
+            const int idx = (q * CH + (REV ? CH - 1 - i : i)) ^ r;
+            const A vv = s_tr[warp][r][idx];
+            s_tr[warp][r][idx] = ex;
+            ex = AR::add(ex, vv);
+          }
+          if (q == (REV ? 0 : LPR - 1)) s_rowagg[kk & 1][warp * RPW + h * RP + r] = incl;
         }
-        A ex = REV ? AR::shfl_down(incl, 1, LPR) : AR::shfl_up(incl, 1, LPR);
-        if (q == (REV ? LPR - 1 : 0)) ex = AR::zero();
+        __syncwarp();
 #pragma unroll
-        for (int i = 0; i < CH; ++i) {
-          const int idx = (q * CH + (REV ? CH - 1 - i : i)) ^ r;
-          const A vv = s_tr[warp][r][idx];
-          s_tr[warp][r][idx] = ex;
-          ex = AR::add(ex, vv);
-        }
-        if (q == (REV ? 0 : LPR - 1)) s_rowagg[kk & 1][warp * RPW + r] = incl;
+        for (int r = 0; r < RP; ++r) E_nxt[h * RP + r] = s_tr[warp][r][lane ^ r];
+        __syncwarp();
       }
-      __syncwarp();
-#pragma unroll
-      for (int r = 0; r < RPW; ++r) E_nxt[r] = s_tr[warp][r][lane ^ r];
-      __syncwarp();
 #pragma unroll
       for (int c = 0; c < CPT; ++c) s_colp[kk & 1][warp][c * 32 + lane] = colp[c];
       return true;
@@ -285,6 +339,33 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
         for (int c = 0; c < CPT; ++c) top[c] = AR::add(base, cp[c]);
       }
       TIn* sb = stages + st * STAGE_ELEMS + (warp * RPW) * TW + lane * CPT;
+      if (DIRECT) {
+        // every input row of the thread into registers, the stage back to the
+        // producer, then the results straight to global memory
+        RowSeg<TIn, CPT> xin[RPW];
+#pragma unroll
+        for (int r = 0; r < RPW; ++r) xin[r].u.v = *reinterpret_cast<const typename RowSeg<TIn, CPT>::V*>(sb + r * TW);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&s_done[st]));
+        const bool vout = (flags & kOutVec) && nvalid == CPT;
+        TOut* out = static_cast<TOut*>(D.out) + (long long)s_pl[st] * D.out_plane + (y0 + warp * RPW) * D.out_pitch + xt;
+#pragma unroll
+        for (int i = 0; i < RPW; ++i) {
+          const int r = REV ? RPW - 1 - i : i;
+          A run = AR::add(E_cur[r], s_rowleft[kb][warp * RPW + r]);
+          TOut o[CPT];
+#pragma unroll
+          for (int ii = 0; ii < CPT; ++ii) {
+            const int c = REV ? CPT - 1 - ii : ii;
+            run = AR::add(run, Cvt<A, TIn>::in(xin[r].u.e[c]));
+            top[c] = AR::add(top[c], run);
+            o[c] = OutCvt<TOut, A>::out(top[c]);
+          }
+          if (y0 + warp * RPW + r < D.height && nvalid > 0) store_seg<TOut, CPT>(out + r * D.out_pitch, vout, nvalid, o);
+        }
+        have = have_next;
+        continue;
+      }
       TOut* so = reinterpret_cast<TOut*>(stages + st * STAGE_ELEMS) + (warp * RPW) * TW + lane * CPT;
       const bool tma_out = flags & kOutTma;
       RowSeg<TIn, CPT> raw[WIDEN ? RPW : 1];
@@ -331,14 +412,19 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
     }
   }
 
-  if (warp == WCOL) {
-    // ---- column warp: column aggregates, exclusive prefix over the warps, the
-    //      column look-back; lane 0 also the corner ------------------------------
+  if (warp >= WCOL && warp < WROW) {
+    // ---- column group: one column (slot) per thread; thread 0 also the corner --
+    const int j = tid - WCOL * 32;
     for (int k = 0;; ++k) {
-      named_sync(kBarAgg0 + (k & 1), NAGG); // tile k's partials are in
       const int st = k % S;
+      // the tile is known once its input has arrived: read the first look-back
+      // windows now, so that round trip overlaps the compute warps' local phase
+      mbar_wait_bounded(smem_u32(&s_full[st]), (k / S) & 1, P, -1);
       const long long t = s_tile[st];
-      if (t < 0) break;
+      if (t < 0) {
+        named_sync(kBarAgg0 + (k & 1), NAGG); // the compute warps' last arrival
+        break;
+      }
       const int kb = k & 1;
       const int ty = s_ty[st];
       const ImageView D = image_view(P, s_img[st]);
@@ -346,52 +432,42 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
       const bool pub_col = (REV ? (ty > 0) : (ty < nty - 1)) && t != P.stall_tile;
       const long long cstride = (REV ? 1 : -1) * (long long)ntx * TW * K;
       const int csteps = REV ? (nty - 1 - ty) : ty;
-      EarlyWin<A> win[COLS_PER_LANE];
-#pragma unroll
-      for (int i = 0; i < COLS_PER_LANE; ++i)
-        early_read<A>(win[i], P.col_words + ((unsigned long long)t * TW + lane + 32 * i) * K, cstride, csteps);
-      EarlyWin<A> cwin;
+      unsigned long long* base = P.col_words + ((unsigned long long)t * TW + j) * K;
+      EarlyWin<A> win[1];
+      early_read<A>(win[0], base, cstride, csteps);
+      EarlyWin<A> cwin[1];
       unsigned long long* cbase = P.corner_words + (unsigned long long)t * K;
       const long long kstride = (REV ? 1 : -1) * (long long)ntx * K;
-      if (lane == 0) early_read<A>(cwin, cbase, kstride, csteps);
-      A agg[COLS_PER_LANE];
+      if (j == 0) early_read<A>(cwin[0], cbase, kstride, csteps);
+      named_sync(kBarAgg0 + kb, NAGG); // tile k's partials are in
+      // the column's partials of every compute warp: all loads first, then the
+      // exclusive prefix over the warps (scan order) and the aggregate
+      A v[NWC];
 #pragma unroll
-      for (int i = 0; i < COLS_PER_LANE; ++i) {
-        const int j = lane + 32 * i;
-        A ac = AR::zero();
+      for (int w = 0; w < NWC; ++w) v[w] = s_colp[kb][w][j];
+      A run = AR::zero();
 #pragma unroll
-        for (int w = 0; w < NWC; ++w) ac = AR::add(ac, s_colp[kb][w][j]);
-        if (pub_col) publish<A>(P.col_words + ((unsigned long long)t * TW + j) * K, ac, tagA);
-        A run = AR::zero();
-#pragma unroll
-        for (int ii = 0; ii < NWC; ++ii) {
-          const int w = REV ? NWC - 1 - ii : ii;
-          const A b = s_colp[kb][w][j];
-          s_colp[kb][w][j] = run;
-          run = AR::add(run, b);
-        }
-        agg[i] = ac;
+      for (int i = 0; i < NWC; ++i) {
+        const int w = REV ? NWC - 1 - i : i;
+        s_colp[kb][w][j] = run;
+        run = AR::add(run, v[w]);
       }
-      // all of this lane's columns resolve together (their round trips overlap)
-      A above[COLS_PER_LANE];
-      resolve_n<A, COLS_PER_LANE>(win, P.col_words + ((unsigned long long)t * TW + lane) * K, 32LL * K, cstride,
-                                  csteps, tagA, tagI, P, t, above);
-#pragma unroll
-      for (int i = 0; i < COLS_PER_LANE; ++i) {
-        const int j = lane + 32 * i;
-        unsigned long long* base = P.col_words + ((unsigned long long)t * TW + j) * K;
-        if (pub_col) publish<A>(base, AR::add(above[i], agg[i]), tagI);
-        s_colabove[kb][j] = above[i];
-      }
-      if (lane == 0) {
-        const A c = resolve<A>(cwin, cbase, kstride, csteps, tagA, tagI, P, t);
-        vstore(&s_corner[kb], c);
+      const A agg = run;
+      if (pub_col) publish<A>(base, agg, tagA);
+      A above[1];
+      resolve_n<A, 1>(win, base, 0, cstride, csteps, tagA, tagI, P, t, above);
+      if (pub_col) publish<A>(base, AR::add(above[0], agg), tagI);
+      s_colabove[kb][j] = above[0];
+      if (j == 0) {
+        A c[1];
+        resolve_n<A, 1>(cwin, cbase, 0, kstride, csteps, tagA, tagI, P, t, c);
+        vstore(&s_corner[kb], c[0]);
         __threadfence_block();
         if (atomicAdd(&s_cnt_corner[kb], 1) == 1) {
           // u is in: this thread publishes corner + u
           __threadfence_block();
           s_cnt_corner[kb] = 0;
-          if (pub_col) publish<A>(cbase, AR::add(c, vload(&s_u[kb])), tagI);
+          if (pub_col) publish<A>(cbase, AR::add(c[0], vload(&s_u[kb])), tagI);
         }
       }
       __syncwarp();
@@ -399,13 +475,18 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
     }
   }
 
-  if (warp == WROW) {
-    // ---- row warp: row aggregates, the row look-back, rowleft's scan and u ---
+  if (warp >= WROW && warp < WSTORE) {
+    // ---- row group: one row per thread; rowleft's scan over the tile's rows and u
+    const int y = tid - WROW * 32; // the thread's row
+    const int rw = warp - WROW;    // its warp within the group
     for (int k = 0;; ++k) {
-      named_sync(kBarAgg0 + (k & 1), NAGG);
       const int st = k % S;
+      mbar_wait_bounded(smem_u32(&s_full[st]), (k / S) & 1, P, -1);
       const long long t = s_tile[st];
-      if (t < 0) break;
+      if (t < 0) {
+        named_sync(kBarAgg0 + (k & 1), NAGG);
+        break;
+      }
       const int kb = k & 1;
       const int tx = s_tx[st], ty = s_ty[st];
       const ImageView D = image_view(P, s_img[st]);
@@ -415,54 +496,42 @@ __global__ void __launch_bounds__((NWC + 3) * 32, 1) sat_tile_kernel_ws(const __
       const bool pub_col = (REV ? (ty > 0) : (ty < nty - 1)) && !stall;
       const long long rstride = (REV ? 1 : -1) * (long long)TH * K;
       const int rsteps = REV ? (ntx - 1 - tx) : tx;
-      EarlyWin<A> win[ROWS_PER_LANE];
-      A agg[ROWS_PER_LANE], left[ROWS_PER_LANE];
-#pragma unroll
-      for (int i = 0; i < ROWS_PER_LANE; ++i) {
-        const int y = lane * ROWS_PER_LANE + i;
-        unsigned long long* base = P.row_words + ((unsigned long long)t * TH + y) * K;
-        early_read<A>(win[i], base, rstride, rsteps);
-        agg[i] = s_rowagg[kb][y];
-        if (pub_row) publish<A>(base, agg[i], tagA);
-      }
-      resolve_n<A, ROWS_PER_LANE>(win, P.row_words + ((unsigned long long)t * TH + lane * ROWS_PER_LANE) * K, K,
-                                  rstride, rsteps, tagA, tagI, P, t, left);
-#pragma unroll
-      for (int i = 0; i < ROWS_PER_LANE; ++i) {
-        const int y = lane * ROWS_PER_LANE + i;
-        unsigned long long* base = P.row_words + ((unsigned long long)t * TH + y) * K;
-        if (pub_row) publish<A>(base, AR::add(left[i], agg[i]), tagI);
-        s_rowleft[kb][y] = left[i];
-      }
-      // inclusive scan of rowleft over the tile's rows, in scan order
-      A incl[ROWS_PER_LANE];
-      A tsum = AR::zero();
-#pragma unroll
-      for (int ii = 0; ii < ROWS_PER_LANE; ++ii) {
-        const int i = REV ? ROWS_PER_LANE - 1 - ii : ii;
-        tsum = AR::add(tsum, left[i]);
-        incl[i] = tsum;
-      }
-      A lsum = tsum; // inclusive over the lanes (scan order)
+      unsigned long long* base = P.row_words + ((unsigned long long)t * TH + y) * K;
+      EarlyWin<A> win[1];
+      early_read<A>(win[0], base, rstride, rsteps);
+      named_sync(kBarAgg0 + kb, NAGG);
+      const A agg = s_rowagg[kb][y];
+      if (pub_row) publish<A>(base, agg, tagA);
+      A left[1];
+      resolve_n<A, 1>(win, base, 0, rstride, rsteps, tagA, tagI, P, t, left);
+      if (pub_row) publish<A>(base, AR::add(left[0], agg), tagI);
+      s_rowleft[kb][y] = left[0];
+      // inclusive scan of rowleft over the tile's rows, in scan order: within
+      // the warp, then across the group's warps
+      A incl = left[0];
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
-        const A o = REV ? AR::shfl_down(lsum, d) : AR::shfl_up(lsum, d);
-        if (REV ? (lane + d < 32) : (lane >= d)) lsum = AR::add(o, lsum);
+        const A o = REV ? AR::shfl_down(incl, d) : AR::shfl_up(incl, d);
+        if (REV ? (lane + d < 32) : (lane >= d)) incl = AR::add(o, incl);
       }
-      A lex = REV ? AR::shfl_down(lsum, 1) : AR::shfl_up(lsum, 1);
-      if (lane == (REV ? 31 : 0)) lex = AR::zero();
+      if (NRW > 1) {
+        if (lane == (REV ? 0 : 31)) s_rwt[kb][rw] = incl;
+        named_sync(kBarRows, NRW * 32);
+        A before = AR::zero();
 #pragma unroll
-      for (int i = 0; i < ROWS_PER_LANE; ++i) {
-        incl[i] = AR::add(lex, incl[i]);
-        const int y = lane * ROWS_PER_LANE + i;
-        // rowleft summed over the rows before compute warp w (scan order)
-        if (!REV && (y + 1) % RPW == 0 && y + 1 < TH) s_rlprev[kb][(y + 1) / RPW] = incl[i];
-        if (REV && y % RPW == 0 && y > 0) s_rlprev[kb][y / RPW - 1] = incl[i];
+        for (int i = 0; i < NRW; ++i) {
+          const int w = REV ? NRW - 1 - i : i;
+          if (REV ? (w > rw) : (w < rw)) before = AR::add(before, s_rwt[kb][w]);
+        }
+        incl = AR::add(before, incl);
       }
-      if (lane == 0) s_rlprev[kb][REV ? NWC - 1 : 0] = AR::zero();
+      // rowleft summed over the rows before compute warp w (scan order)
+      if (!REV && (y + 1) % RPW == 0 && y + 1 < TH) s_rlprev[kb][(y + 1) / RPW] = incl;
+      if (REV && y % RPW == 0 && y > 0) s_rlprev[kb][y / RPW - 1] = incl;
+      if (y == (REV ? TH - 1 : 0)) s_rlprev[kb][REV ? NWC - 1 : 0] = AR::zero();
       // u = sum of rowleft: the corner aggregate of the tile below
-      if (lane == (REV ? 0 : 31)) {
-        const A u = incl[REV ? 0 : ROWS_PER_LANE - 1];
+      if (y == (REV ? 0 : TH - 1)) {
+        const A u = incl;
         unsigned long long* cw = P.corner_words + (unsigned long long)t * K;
         if (pub_col) publish<A>(cw, u, tagA);
         vstore(&s_u[kb], u);

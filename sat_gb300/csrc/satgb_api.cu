@@ -26,11 +26,12 @@
 namespace satgb {
 
 const TileConfig kConfigs[kNumConfigs] = {
-    {4, 16, "warp-specialized: 64-row tiles, 16 compute warps, column/row look-back and store warps"},
+    {4, 16, "warp-specialized: 64-row tiles, one look-back thread per row and column"},
     {8, 16, "pipelined: 128-row tiles (64 for 8-byte accumulators), 16 warps"},
     {8, 8, "pipelined: 64-row tiles (32 for 8-byte accumulators), 8 warps, 2 CTAs per SM"},
     {8, 16, "registers: 128-row tiles, 16 warps"},
     {16, 16, "pipelined, 256-row tiles, direct stores (1-byte inputs, 4-byte sums)"},
+    {8, 16, "warp-specialized, direct stores: 128-row tiles (64 for 8-byte accumulators)"},
 };
 
 namespace {
@@ -464,37 +465,50 @@ int sms_of(int dev) {
   return d.sms;
 }
 
-// Heuristic default when no tuning entry exists: the largest tiles that
-// still give every SM several of them.
-// Untuned choice, from measurements on GB300 at 8192^2 (f32) and 4096^2 (f64).
-// 4-byte accumulators: the 128-row pipelined tiles when there are enough of
-// them to fill the GPU a few times over, else the 64-row two-CTA tiles.
-// Compensated f32: the 128-row register tiles.
+// Heuristic default when no tuning entry exists, from measurements on GB300
+// (CUDA events, square images 1024^2 .. 32768^2):
+// 4-byte accumulators: the warp-specialized direct-store tiles (configuration
+// 5) once there are at least 4 tiles of 128 x 128 per SM (f32: 2959 vs 2851
+// GB/s at 4096^2, 4521 vs 3893 at 8192^2, 5510 vs 4370 at 16384^2), else the
+// 128-row pipelined tiles (1494 vs 1369 GB/s at 2048^2).
+// 1-byte inputs with 4-byte sums: configuration 5 from 16 tiles per SM (3185
+// vs 3093 GB/s at 8192^2, 4022 vs 3518 at 16384^2, 4358 vs 3621 at 32768^2),
+// the 256-row direct-store tiles below that (2159 vs 2051 at 4096^2).
+// Compensated f32: the 128-row register tiles (2474 vs 1570 GB/s for
+// configuration 5 at 8192^2, 1096 vs 911 for the 64-row tiles at 2048^2).
 // f64 outputs (slow FP64 adds on GB300): the warp-specialized tiles, whose
 // compute warps never wait at a CTA barrier.
-// 1-byte inputs with 4-byte sums: the 256-row direct-store tiles from 2048²
-// up (measured +10 % at 2048², +23 % at 8192², +27 % at 32768² over the
-// 128-row tiles).
-int default_config(long long width, long long height, int sms, int in_sz, int out_sz, bool compensated) {
+// Stacks of planes count all their tiles for the size classes, but
+// configuration 5 needs its tile count in one plane: its gain is in long
+// look-back chains, and stacks of small planes (64 x 3 planes of 1024^2, the
+// box-filter layer) ran 15 % slower with it than with the pipelined tiles.
+int default_config(long long width, long long height, int sms, int in_sz, int out_sz, bool compensated,
+                   long long planes = 1) {
   const int cpt = 16 / out_sz;
   const long long tw = 32LL * cpt;
   const long long ntx = (width + tw - 1) / tw;
-  const long long tiles128 = ntx * ((height + 127) / 128);
+  const long long plane_tiles = ntx * ((height + 127) / 128);
+  const long long tiles128 = plane_tiles * std::max(1LL, planes);
   sms = std::max(1, sms);
-  const bool large = tiles128 >= 8LL * sms;
-  if (out_sz == 8) return large ? 0 : 2;
-  if (compensated) return large ? 3 : 2;
-  if (in_sz == 1 && ntx * ((height + 255) / 256) >= 64) return 4;
-  return large ? 1 : 2;
+  if (out_sz == 8) return tiles128 >= 8LL * sms ? 0 : 2;
+  if (compensated) return tiles128 >= sms ? 3 : 2;
+  if (in_sz == 1) {
+    if (plane_tiles >= 16LL * sms) return 5;
+    if (ntx * ((height + 255) / 256) * std::max(1LL, planes) >= 64) return 4;
+    return 1;
+  }
+  return plane_tiles >= 4LL * sms ? 5 : 1;
 }
 
-int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, long long h, int dev) {
+int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, long long h, int dev,
+                         long long planes = 1) {
   if (g_forced_config >= 0) return g_forced_config;
   tune_load_locked();
   const int sms = sms_of(dev);
-  auto it = g_tune.find(TuneKey(in_t, out_t, mode, dir, log2_bucket(w), log2_bucket(h), sms));
+  auto it = g_tune.find(TuneKey(in_t, out_t, mode, dir, log2_bucket(w), log2_bucket(h * std::max(1LL, planes)), sms));
   if (it != g_tune.end()) return it->second;
-  return default_config(w, h, sms, (int)dtype_size(in_t), (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED);
+  return default_config(w, h, sms, (int)dtype_size(in_t), (int)dtype_size(out_t), mode == SATGB_MODE_COMPENSATED,
+                        planes);
 }
 
 satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const ImageDesc& img0,
@@ -569,12 +583,12 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   if (st != SATGB_OK) return st;
   int cfg = force_cfg >= 0 ? force_cfg
             : (mode >= kModeRows) ? 1
-                                  : choose_config_locked(in_t, out_t, mode, dir, width, height * std::max(1LL, planes), dev);
+                                  : choose_config_locked(in_t, out_t, mode, dir, width, height, dev, planes);
   const Variant* v = find_variant(in_t, out_t, mode, dir, cfg);
   if (!v && mode < kModeRows) // a configuration this pair does not have: the untuned choice
     v = find_variant(in_t, out_t, mode, dir,
-                     default_config(width, height * std::max(1LL, planes), sms_of(dev), (int)in_sz, (int)out_sz,
-                                    mode == SATGB_MODE_COMPENSATED));
+                     default_config(width, height, sms_of(dev), (int)in_sz, (int)out_sz,
+                                    mode == SATGB_MODE_COMPENSATED, planes));
   if (!v) v = find_variant(in_t, out_t, mode, dir, 0);
   if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for %s -> %s mode %d dir %d", dtype_name(in_t), dtype_name(out_t), mode, dir);
   ImageDesc d;
