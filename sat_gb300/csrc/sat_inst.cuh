@@ -5,6 +5,7 @@
 #include "sat_kernel.cuh"
 #include "sat_kernel_r.cuh"
 #include "sat_kernel_ws.cuh"
+#include "sat_kernel_rm.cuh"
 #include "sat_registry.h"
 
 namespace satgb {
@@ -120,6 +121,41 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
                  SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
 }
 
+// The same three for sat_tile_kernel_rm (row-major tile order, direct stores).
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+cudaError_t prepare_impl_rm() {
+  using SH = TileShapeRM<TIn, TOut, A, RPW, NWC>;
+  constexpr int kMaxDev = 64;
+  static std::atomic<int> done[kMaxDev];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < kMaxDev && done[dev].load(std::memory_order_acquire)) return cudaSuccess;
+  e = cudaFuncSetAttribute(&sat_tile_kernel_rm<TIn, TOut, A, REV, RPW, NWC>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, SH::DYN_SMEM);
+  if (e == cudaSuccess && dev >= 0 && dev < kMaxDev) done[dev].store(1, std::memory_order_release);
+  return e;
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+cudaError_t launch_impl_rm(const SatParams& p, int grid, cudaStream_t s) {
+  using SH = TileShapeRM<TIn, TOut, A, RPW, NWC>;
+  cudaError_t e = prepare_impl_rm<TIn, TOut, A, REV, RPW, NWC>();
+  if (e != cudaSuccess) return e;
+  sat_tile_kernel_rm<TIn, TOut, A, REV, RPW, NWC><<<grid, SH::THREADS, SH::DYN_SMEM, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <class TIn, class TOut, class A, bool REV, int RPW, int NWC>
+Variant make_variant_rm(int in_t, int out_t, int mode, int cfg) {
+  using SH = TileShapeRM<TIn, TOut, A, RPW, NWC>;
+  return Variant{in_t, out_t, mode, REV ? 1 : 0, cfg,
+                 &launch_impl_rm<TIn, TOut, A, REV, RPW, NWC>,
+                 &prepare_impl_rm<TIn, TOut, A, REV, RPW, NWC>,
+                 (const void*)&sat_tile_kernel_rm<TIn, TOut, A, REV, RPW, NWC>,
+                 SH::TH, SH::TW, Ar<A>::K, SH::THREADS, SH::DYN_SMEM};
+}
+
 }  // namespace satgb
 
 // dtype codes (satgb_dtype)
@@ -143,6 +179,8 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
 //   5: warp-specialized with direct stores, 8 rows a compute warp: 128-row
 //      tiles and 16 compute warps for 4-byte accumulators (64-row tiles and 8
 //      compute warps for 8-byte ones)
+//   6: as 5, with the tiles in row-major order: rowleft is the sum of every
+//      row aggregate to the left, the look-back is vertical only (no corner)
 #define SG_CFG1_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_R0_RPW(A) (sizeof(A) == 8 ? 4 : 8)
 #define SG_WS_RPW(A) (sizeof(A) == 8 ? 8 : 4)  /* 64-row tiles either way: */
@@ -152,7 +190,8 @@ Variant make_variant_ws(int in_t, int out_t, int mode, int cfg) {
       satgb::make_variant<TIN, TOUT, A, REV, SG_CFG1_RPW(A), 16, 1>(IT, OT, MODE, 1),    \
       satgb::make_variant<TIN, TOUT, A, REV, SG_R0_RPW(A), 8, 2>(IT, OT, MODE, 2),       \
       satgb::make_variant_r<TIN, TOUT, A, REV, 8, 16, 1>(IT, OT, MODE, 3),               \
-      satgb::make_variant_ws<TIN, TOUT, A, REV, 8, SG_WS_NWC(A), true>(IT, OT, MODE, 5)
+      satgb::make_variant_ws<TIN, TOUT, A, REV, 8, SG_WS_NWC(A), true>(IT, OT, MODE, 5),   \
+      satgb::make_variant_rm<TIN, TOUT, A, REV, 8, SG_WS_NWC(A)>(IT, OT, MODE, 6)
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
   SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
 

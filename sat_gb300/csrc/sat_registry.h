@@ -33,7 +33,7 @@ struct TileConfig {
   int warps;
   const char* name;
 };
-constexpr int kNumConfigs = 6;
+constexpr int kNumConfigs = 7;
 extern const TileConfig kConfigs[kNumConfigs];
 
 // Lists of variants, one per instantiation translation unit.

@@ -32,6 +32,7 @@ const TileConfig kConfigs[kNumConfigs] = {
     {8, 16, "registers: 128-row tiles, 16 warps"},
     {16, 16, "pipelined, 256-row tiles, direct stores (1-byte inputs, 4-byte sums)"},
     {8, 16, "warp-specialized, direct stores: 128-row tiles (64 for 8-byte accumulators)"},
+    {8, 16, "warp-specialized, direct stores, row-major tile order: 128-row tiles (64 for 8-byte accumulators)"},
 };
 
 namespace {

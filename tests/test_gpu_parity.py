@@ -89,7 +89,7 @@ SHAPES = [(1, 1), (1, 700), (700, 1), (2, 3), (63, 127), (64, 128), (65, 129), (
           (129, 257), (300, 1000), (1000, 300), (517, 769)]
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5, 6])
 def test_all_pairs_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -103,7 +103,7 @@ def test_all_pairs_all_configs(cuda, oracle, cfg):
         sat_gb300.set_config(-1)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5, 6])
 def test_reverse_all_configs(cuda, oracle, cfg):
     sat_gb300.set_config(cfg)
     try:
@@ -332,7 +332,7 @@ def test_full_size_u8_properties_and_configs_agree(cuda):
     assert torch.equal(s_def[:, -1].to(torch.int64), row)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5, 6])
 def test_timeout_is_reported_and_context_survives(cuda, oracle, cfg):
     """A tile that never publishes makes its dependents hit the wait limit
     (every kernel: warp-specialized, pipelined, register-resident); the call
