@@ -526,6 +526,9 @@ def batch_result(dev, stream, peak, pitched=True):
     import sat_gb300
     xs, ys, nbytes = build_batch(dev, pitched=pitched)
     plan = sat_gb300.BatchPlan(xs, ys, stream=stream)
+    _, per_u = _time_steps(lambda: plan.exec(stream), 10, 3, stream, 0.1)
+    untuned = [c["config"] for c in plan.classes()]
+    plan.autotune(stream)
     _, per_g = _time_steps(lambda: plan.exec(stream), 20, 3, stream, 0.2)
     plan.check(stream)
 
@@ -539,7 +542,9 @@ def batch_result(dev, stream, peak, pitched=True):
     res = {"images": len(xs), "bytes": int(nbytes), "graph_ms": round(gm, 4),
            "graph_gbs": round(nbytes / (gm / 1e3) / GB, 1), "frac_of_peak": round(nbytes / (gm / 1e3) / GB / peak, 4),
            "per_image_ms": round(im, 4), "per_image_gbs": round(nbytes / (im / 1e3) / GB, 1),
-           "tiles": plan.info()["n_tiles"], "rows": "pitched to 128 B" if pitched else "packed"}
+           "tiles": plan.info()["n_tiles"], "rows": "pitched to 128 B" if pitched else "packed",
+           "classes": plan.classes(), "untuned_configs": untuned,
+           "untuned_graph_gbs": round(nbytes / (statistics.median(per_u) / 1e3) / GB, 1)}
     plan.close()
     return res
 
@@ -621,11 +626,14 @@ def run_workload(args):
             sat_gb300.set_config(args.config)
         xs, ys, nbytes = build_batch(dev, pitched=args.case == "batch512")
         plan = sat_gb300.BatchPlan(xs, ys, stream=stream)
+        if args.tune:
+            plan.autotune(stream)
         _, per = _time_steps(lambda: plan.exec(stream), args.steps, args.warmup, stream, 0.0)
         plan.check(stream)
         med = statistics.median(per)
         print(json.dumps({"case": args.case, "config": plan.info()["config"], "tiles": plan.info()["n_tiles"],
-                          "ms_median": round(med, 5), "gbs": round(nbytes / (med / 1e3) / GB, 1)}))
+                          "classes": plan.classes(), "ms_median": round(med, 5),
+                          "gbs": round(nbytes / (med / 1e3) / GB, 1)}))
     elif args.case in ("box_fwd", "box_fwdbwd"):
         n = 8 if args.small else 64
         x, wts, radii = build_box(dev, n=n)
@@ -674,6 +682,7 @@ def main():
     ap.add_argument("--small", action="store_true", help="box workloads: 8 images instead of 64")
     ap.add_argument("--no-extra", action="store_true", help="skip the batch, box-filter and stress sub-results")
     ap.add_argument("--config", type=int, default=-1, help="force a tile configuration (--case only)")
+    ap.add_argument("--tune", action="store_true", help="batch cases: run the batch autotuner first")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)

@@ -215,12 +215,15 @@ satgb_status satgb_box_filter_bwd(const satgb_box_desc* desc, satgb_stream strea
 satgb_status satgb_sat_noalloc(const satgb_sat_desc* desc, satgb_stream stream);
 
 /* ------------------------------------------------------------------------- */
-/* Batched SAT: many images of uneven sizes, one persistent launch.           */
-/* No reference counterpart (the reference's drivers handle one image).       */
-/* A plan copies the image table to the device, picks a tile configuration    */
-/* (from the autotuner's cache when an entry exists) and captures the launch  */
-/* in a CUDA graph; exec replays the graph on `stream`.  All images share one */
-/* dtype pair, mode and direction.                                            */
+/* Batched SAT: many images of uneven sizes, one persistent launch per size   */
+/* class.  No reference counterpart (the reference's drivers handle one       */
+/* image).  A plan copies the image table to the device, splits the images    */
+/* into two size classes (large: at least 64 tiles of 128 x 128 pixels;       */
+/* small: the rest), picks a tile configuration per class (from the tuning    */
+/* cache when an entry for this batch's signature exists) and captures the    */
+/* classes' launches, one after the other, in one CUDA graph; exec replays    */
+/* the graph on `stream`.  All images share one dtype pair, mode and          */
+/* direction.  No image may write memory another image reads or writes.       */
 /* ------------------------------------------------------------------------- */
 typedef struct {
   const void* d_in;
@@ -236,11 +239,23 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
                                      int mode, int direction, const satgb_image* images,
                                      int64_t n_images, satgb_stream stream);
 satgb_status satgb_batch_plan_exec(satgb_batch_plan* plan, satgb_stream stream);
-/* Launch without the graph (same kernel, same arguments). */
+/* Launch without the graph (same kernels, same arguments). */
 satgb_status satgb_batch_plan_launch(satgb_batch_plan* plan, satgb_stream stream);
 satgb_status satgb_batch_plan_destroy(satgb_batch_plan* plan);
-/* Tiles in the plan and the configuration index it uses. */
+/* Tiles in the plan and the configuration index of its large class (of the
+ * small class when there are no large images). */
 satgb_status satgb_batch_plan_info(const satgb_batch_plan* plan, int64_t* n_tiles, int* config);
+/* Per size class (index 0 large, 1 small): images, tiles and configuration
+ * (-1 for an empty class).  Each pointer may be NULL or point to 2 values. */
+satgb_status satgb_batch_plan_classes(const satgb_batch_plan* plan, int64_t* n_images, int64_t* n_tiles,
+                                      int* configs);
+/* Batch autotuner: times every tile configuration of each size class on the
+ * plan's own images (launches whose results overwrite the outputs), keeps the
+ * fastest, records it in the tuning cache under the batch's signature (dtype
+ * pair, mode, direction, class, pixel and image counts, TMA alignment of the
+ * rows, SM count; persisted in SATGB_TUNE_CACHE when set) and captures the
+ * plan's graph again.  configs may be NULL or receive the 2 chosen indices. */
+satgb_status satgb_batch_plan_autotune(satgb_batch_plan* plan, satgb_stream stream, int* configs);
 /* Synchronises `stream` and reports (and clears) a device-side error of the
  * plan's launches, like satgb_stream_check does for single-image calls. */
 satgb_status satgb_batch_plan_check(satgb_batch_plan* plan, satgb_stream stream);

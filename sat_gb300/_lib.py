@@ -88,6 +88,8 @@ SIGNATURES = {
     "satgb_batch_plan_destroy": (_ST, [_P]),
     "satgb_batch_plan_info": (_ST, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
     "satgb_batch_plan_check": (_ST, [_P, _P]),
+    "satgb_batch_plan_classes": (_ST, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
+    "satgb_batch_plan_autotune": (_ST, [_P, _P, ctypes.POINTER(_I)]),
     "satgb_autotune": (_ST, [_I, _I, _I, _P, _I64, _P, _I64, _I64, _I64, _P, ctypes.POINTER(_I)]),
     "satgb_num_configs": (_I, []),
     "satgb_config_name": (ctypes.c_char_p, [_I]),

@@ -334,6 +334,22 @@ class BatchPlan:
         check(_lib.load().satgb_batch_plan_info(self._plan, ctypes.byref(n), ctypes.byref(c)))
         return {"n_tiles": n.value, "config": c.value}
 
+    def classes(self):
+        """Per size class (large, small): image count, tiles and configuration."""
+        n = (ctypes.c_int64 * 2)()
+        t = (ctypes.c_int64 * 2)()
+        c = (ctypes.c_int * 2)()
+        check(_lib.load().satgb_batch_plan_classes(self._plan, n, t, c))
+        return [{"images": n[i], "tiles": t[i], "config": c[i]} for i in range(2)]
+
+    def autotune(self, stream=None):
+        """Times every tile configuration per size class on this plan's images
+        (overwriting the outputs), keeps the fastest and records it in the
+        tuning cache; returns the chosen configurations (large, small)."""
+        c = (ctypes.c_int * 2)()
+        check(_lib.load().satgb_batch_plan_autotune(self._plan, _stream_handle(stream), c))
+        return (c[0], c[1])
+
     def close(self) -> None:
         if self._plan:
             _lib.load().satgb_batch_plan_destroy(self._plan)

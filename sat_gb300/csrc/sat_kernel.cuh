@@ -99,6 +99,10 @@ struct SatParams {
   WsHeader* ws;
   int64_t wait_limit_ns;
   int64_t stall_tile; // test knob: this tile never publishes (-1: none)
+  // Batches: the tile of each ticket, (image << 40) | (ty << 20) | tx, in an
+  // order whose every tile comes after the tiles it depends on (nullptr: the
+  // images one after the other, each in the kernel's own order).
+  const unsigned long long* order;
 };
 
 // Pipeline depth.  A stage holds one tile from its TMA load until its TMA
@@ -177,10 +181,59 @@ __device__ __forceinline__ void store_seg(TOut* p, bool vec, int nvalid, const T
 #pragma unroll
     for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
     __stcs(reinterpret_cast<uint4*>(p), u.v);
+  } else if (CPT * sizeof(TOut) == 16 && nvalid == CPT && ((uintptr_t)p % 16) == 0) {
+    // rows whose pitch is not a multiple of 16 bytes: this row's segment may still be aligned
+    union {
+      uint4 v;
+      TOut e[CPT];
+    } u;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
+    __stcs(reinterpret_cast<uint4*>(p), u.v);
+  } else if (CPT * sizeof(TOut) == 16 && nvalid == CPT && ((uintptr_t)p % 8) == 0) {
+    union {
+      uint2 v[2];
+      TOut e[CPT];
+    } u;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) u.e[c] = o[c];
+    __stcs(reinterpret_cast<uint2*>(p), u.v[0]);
+    __stcs(reinterpret_cast<uint2*>(p) + 1, u.v[1]);
   } else {
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
       if (c < nvalid) __stcs(p + c, o[c]);
+  }
+}
+
+// One row segment of CPT input elements from global memory when the caller's
+// rows are not vector-aligned (packed rows of odd widths, offset views): four
+// 1-byte pixels come from the one or two aligned 32-bit words that hold them
+// (both inside the buffer: each holds a byte of the segment), a 16-byte
+// segment of wider types by one vector load when this row happens to be
+// aligned; else element by element.  Elements past nvalid are zero.
+template <class TIn, int CPT>
+__device__ __forceinline__ void load_seg_unaligned(const TIn* p, int nvalid, TIn (&x)[CPT]) {
+  if (sizeof(TIn) == 1 && CPT == 4) {
+    const uintptr_t a = (uintptr_t)p;
+    const unsigned off = (unsigned)(a & 3u);
+    const uint32_t* wp = reinterpret_cast<const uint32_t*>(a - off);
+    const uint32_t lo = __ldcs(wp);
+    const uint32_t hi = (off + (unsigned)nvalid > 4u) ? __ldcs(wp + 1) : 0u;
+    uint32_t v = __funnelshift_r(lo, hi, off * 8u);
+    if (nvalid < 4) v &= (1u << (8 * nvalid)) - 1u;
+    union {
+      uint32_t w;
+      TIn e[4];
+    } u;
+    u.w = v;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) x[c] = u.e[c < 4 ? c : 0];
+  } else if (nvalid == CPT && ((uintptr_t)p % (CPT * sizeof(TIn))) == 0) {
+    load_seg<TIn, CPT>(p, true, CPT, x);
+  } else {
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) x[c] = (c < nvalid) ? __ldcs(p + c) : TIn(0);
   }
 }
 
@@ -193,12 +246,19 @@ __device__ __forceinline__ void store_seg(TOut* p, bool vec, int nvalid, const T
 template <class TIn, int CPT, int RPW, int TW>
 __device__ __noinline__ void stage_fill(TIn* sb, const TIn* g, long long pitch, int rows, int nvalid, int c0,
                                         bool vec) {
+  // every row's loads first, then the shared-memory stores, so the loads overlap
+  RowSeg<TIn, CPT> seg[RPW];
+#pragma unroll
   for (int r = 0; r < RPW; ++r) {
     TIn x[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) x[c] = TIn(0);
     if (c0 > 0) load_seg_smem<TIn, CPT>(sb + r * TW, x);
     if (r < rows && nvalid > 0) {
       if (vec && c0 == 0 && nvalid == CPT) {
         load_seg<TIn, CPT>(g + r * pitch, true, CPT, x);
+      } else if (c0 == 0) {
+        load_seg_unaligned<TIn, CPT>(g + r * pitch, nvalid, x);
       } else {
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
@@ -209,11 +269,11 @@ __device__ __noinline__ void stage_fill(TIn* sb, const TIn* g, long long pitch, 
       for (int c = 0; c < CPT; ++c)
         if (c >= c0) x[c] = TIn(0);
     }
-    RowSeg<TIn, CPT> seg;
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) seg.u.e[c] = x[c];
-    *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = seg.u.v;
+    for (int c = 0; c < CPT; ++c) seg[r].u.e[c] = x[c];
   }
+#pragma unroll
+  for (int r = 0; r < RPW; ++r) *reinterpret_cast<typename RowSeg<TIn, CPT>::V*>(sb + r * TW) = seg[r].u.v;
 }
 
 template <class TOut, int CPT, int RPW, int TW, bool REV>
@@ -597,6 +657,15 @@ __device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long lon
   tp.tx = tp.ty = tp.img = tp.pl = 0;
   if ((long long)tk >= P.n_tiles) return tp;
   const long long q = REV ? (P.n_tiles - 1 - (long long)tk) : (long long)tk;
+  if (P.order) {
+    const unsigned long long e = P.order[q];
+    tp.img = (int)(e >> 40);
+    tp.ty = (int)((e >> 20) & 0xFFFFFu);
+    tp.tx = (int)(e & 0xFFFFFu);
+    tp.pl = 0;
+    tp.t = P.images[tp.img].tile_base + (long long)tp.ty * P.images[tp.img].ntx + tp.tx;
+    return tp;
+  }
   int img = 0;
   if (P.n_images > 1) {
     int lo = 0, hi = (int)P.n_images - 1; // last image with tile_base <= q

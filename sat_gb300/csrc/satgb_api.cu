@@ -414,6 +414,9 @@ satgb_status check_batch_disjoint(const std::vector<ImgCheck>& imgs, size_t in_s
 // ----------------------------------------------------------------------------
 using TuneKey = std::tuple<int, int, int, int, int, int, int>;
 std::map<TuneKey, int> g_tune;
+// batch plans: (in, out, mode, dir, size class, log2 pixels, log2 images, all rows TMA-able, SMs) -> cfg
+using BatchKey = std::tuple<int, int, int, int, int, int, int, int, int>;
+std::map<BatchKey, int> g_batch_tune;
 bool g_tune_loaded = false;
 
 int log2_bucket(long long x) {
@@ -433,9 +436,15 @@ void tune_load_locked() {
   char line[512];
   while (fgets(line, sizeof line, f)) {
     int a[8];
+    int b[10];
     if (sscanf(line, " {\"in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"wb\":%d,\"hb\":%d,\"sms\":%d,\"cfg\":%d}",
                &a[0], &a[1], &a[2], &a[3], &a[4], &a[5], &a[6], &a[7]) == 8)
       g_tune[TuneKey(a[0], a[1], a[2], a[3], a[4], a[5], a[6])] = a[7];
+    else if (sscanf(line,
+                    " {\"batch_in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"class\":%d,\"pxb\":%d,\"nb\":%d,"
+                    "\"tma\":%d,\"sms\":%d,\"cfg\":%d}",
+                    &b[0], &b[1], &b[2], &b[3], &b[4], &b[5], &b[6], &b[7], &b[8], &b[9]) == 10)
+      g_batch_tune[BatchKey(b[0], b[1], b[2], b[3], b[4], b[5], b[6], b[7], b[8])] = b[9];
   }
   fclose(f);
 }
@@ -450,6 +459,14 @@ void tune_save_locked() {
     fprintf(f, "{\"in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"wb\":%d,\"hb\":%d,\"sms\":%d,\"cfg\":%d}\n",
             std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k), std::get<5>(k),
             std::get<6>(k), kv.second);
+  }
+  for (auto& kv : g_batch_tune) {
+    const BatchKey& k = kv.first;
+    fprintf(f,
+            "{\"batch_in\":%d,\"out\":%d,\"mode\":%d,\"dir\":%d,\"class\":%d,\"pxb\":%d,\"nb\":%d,"
+            "\"tma\":%d,\"sms\":%d,\"cfg\":%d}\n",
+            std::get<0>(k), std::get<1>(k), std::get<2>(k), std::get<3>(k), std::get<4>(k), std::get<5>(k),
+            std::get<6>(k), std::get<7>(k), std::get<8>(k), kv.second);
   }
   fclose(f);
 }
@@ -514,7 +531,7 @@ int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, lo
 
 satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const ImageDesc& img0,
                            long long n_images, long long n_tiles, Workspace& ws, int dev,
-                           cudaStream_t s) {
+                           cudaStream_t s, const unsigned long long* order = nullptr) {
   const Layout L = layout_for(n_tiles, v);
   satgb_status st = ensure_ws(ws, L.total, s);
   if (st != SATGB_OK) return st;
@@ -534,6 +551,7 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
   P.corner_words = (unsigned long long*)(b + L.corner_off);
   P.wait_limit_ns = g_wait_limit_ns.load();
   P.stall_tile = g_stall_tile.load();
+  P.order = order;
 
   cudaError_t e = v->launch(P, grid, s);
   if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
@@ -621,12 +639,30 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
 // ============================================================================
 // Batch plans
 // ============================================================================
-struct satgb_batch_plan_s {
+// The images of a plan fall into two size classes, each run by its own
+// persistent launch with its own tile configuration (both launches follow one
+// another in the plan's CUDA graph, sharing one workspace): large images,
+// whose long look-back chains favour the big warp-specialized tiles, and small
+// ones, where smaller tiles or the row-major order waste less.
+constexpr int kBatchClasses = 2;
+constexpr long long kLargeTiles = 64; // an image of at least 64 tiles of 128 x 128 is large
+
+struct BatchSeg {
   const Variant* v = nullptr;
-  int dev = 0;
+  std::vector<ImgCheck> imgs;
   long long n_images = 0, n_tiles = 0;
+  double pixels = 0;
   ImageDesc img0;
-  ImageDesc* table = nullptr; // device
+  ImageDesc* table = nullptr;          // device: the descriptors, then the tile order
+  unsigned long long* order = nullptr; // inside the same allocation (nullptr: images one after the other)
+};
+
+struct satgb_batch_plan_s {
+  int in_t = 0, out_t = 0, mode = 0, dir = 0;
+  int dev = 0;
+  bool all_tma = true; // every image's rows can go through TMA (16-byte aligned bases and pitches)
+  BatchSeg seg[kBatchClasses];
+  long long n_tiles = 0;
   Workspace ws;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -847,6 +883,171 @@ satgb_status satgb_autotune(satgb_dtype in_t, satgb_dtype out_t, int mode, const
 // ---------------------------------------------------------------------------
 // batch plans
 // ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+BatchKey batch_key(const satgb_batch_plan_s* p, int cls, int sms) {
+  const BatchSeg& g = p->seg[cls];
+  return BatchKey(p->in_t, p->out_t, p->mode, p->dir, cls, log2_bucket((long long)std::max(1.0, g.pixels)),
+                  log2_bucket(std::max(1LL, g.n_images)), p->all_tma ? 1 : 0, sms);
+}
+
+// Untuned choice for a class (GB300, the 512-image u8 batch): large images the
+// warp-specialized direct-store tiles; small images the 64-row two-CTA tiles
+// when rows go through TMA, the row-major tiles when they cannot (packed rows:
+// 1401 vs 1015 GB/s); f64 outputs and the compensated mode as for one image.
+int batch_default_config(const satgb_batch_plan_s* p, int cls) {
+  if (dtype_size(p->out_t) == 8) return 0;
+  if (p->mode == SATGB_MODE_COMPENSATED) return 3;
+  if (cls == 0) return 5;
+  return p->all_tma ? 2 : 6;
+}
+
+void seg_free(BatchSeg& g) {
+  if (g.table) cudaFree(g.table);
+  g.table = nullptr;
+  g.order = nullptr;
+}
+
+// The tile order of a class: every tile of every image by anti-diagonal
+// (tx + ty) first, then by image, then by row.  A tile's left and upper
+// neighbours lie on the previous diagonal of the same image, so they come
+// earlier (the persistent grid cannot deadlock), and the look-back wavefronts
+// of all the images advance together instead of one image after another,
+// whose chains of dependent tiles would otherwise leave most SMs waiting.
+// Empty when a tile coordinate or an image index does not fit the encoding.
+std::vector<unsigned long long> diagonal_order(const std::vector<ImageDesc>& table) {
+  std::vector<unsigned long long> order;
+  if (table.size() >= (1ULL << 24)) return order;
+  long long maxd = 0, n = 0;
+  for (auto& d : table) {
+    if (d.ntx >= (1 << 20) || d.nty >= (1 << 20)) return order;
+    maxd = std::max(maxd, (long long)d.ntx + d.nty - 1);
+    n += (long long)d.ntx * d.nty;
+  }
+  // counting sort by diagonal, images and rows in order within a diagonal
+  std::vector<long long> count(maxd + 1, 0);
+  for (auto& d : table)
+    for (long long dd = 0; dd < (long long)d.ntx + d.nty - 1; ++dd) {
+      const long long lo = std::max(0LL, dd - (d.ntx - 1)), hi = std::min<long long>(dd, d.nty - 1);
+      count[dd] += hi - lo + 1;
+    }
+  std::vector<long long> start(maxd + 1, 0);
+  for (long long dd = 1; dd <= maxd; ++dd) start[dd] = start[dd - 1] + count[dd - 1];
+  order.assign(n, 0ull);
+  for (size_t i = 0; i < table.size(); ++i) {
+    const ImageDesc& d = table[i];
+    for (long long dd = 0; dd < (long long)d.ntx + d.nty - 1; ++dd) {
+      const long long lo = std::max(0LL, dd - (d.ntx - 1)), hi = std::min<long long>(dd, d.nty - 1);
+      for (long long ty = lo; ty <= hi; ++ty)
+        order[start[dd]++] = ((unsigned long long)i << 40) | ((unsigned long long)ty << 20) | (unsigned long long)(dd - ty);
+    }
+  }
+  return order;
+}
+
+// (Re)builds a class's descriptor table for the configuration `cfg`; called
+// with g_mu held.
+satgb_status seg_build(satgb_batch_plan_s* p, int cls, int cfg, cudaStream_t s) {
+  BatchSeg& g = p->seg[cls];
+  const Variant* v = find_variant(p->in_t, p->out_t, p->mode, p->dir, cfg);
+  if (!v) v = find_variant(p->in_t, p->out_t, p->mode, p->dir, batch_default_config(p, cls));
+  if (!v) v = find_variant(p->in_t, p->out_t, p->mode, p->dir, 0);
+  if (!v) return fail(SATGB_ERR_UNSUPPORTED_TYPES, "no kernel for this batch");
+  std::vector<ImageDesc> table;
+  long long base = 0;
+  for (auto& c : g.imgs) {
+    ImageDesc d;
+    fill_image_desc(d, v, p->in_t, p->out_t, c.in, c.out, c.in_pitch, c.out_pitch, c.width, c.height, base, 1, 0, 0);
+    base += (long long)d.ntx * d.nty;
+    table.push_back(d);
+  }
+  seg_free(g);
+  g.v = v;
+  g.n_tiles = base;
+  if (table.empty()) return SATGB_OK;
+  g.img0 = table[0];
+  const std::vector<unsigned long long> order = table.size() > 1 ? diagonal_order(table) : std::vector<unsigned long long>();
+  const size_t tbytes = (table.size() * sizeof(ImageDesc) + 255) & ~(size_t)255;
+  if (cudaMalloc(&g.table, tbytes + order.size() * sizeof(unsigned long long)) != cudaSuccess) {
+    cudaGetLastError();
+    g.table = nullptr;
+    return fail(SATGB_ERR_ALLOC, "image table allocation failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(g.table, table.data(), table.size() * sizeof(ImageDesc), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && !order.empty()) {
+    g.order = reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(g.table) + tbytes);
+    e = cudaMemcpyAsync(g.order, order.data(), order.size() * sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "image table upload");
+  return SATGB_OK;
+}
+
+satgb_status plan_ws(satgb_batch_plan_s* p, cudaStream_t s) {
+  size_t need = 0;
+  p->n_tiles = 0;
+  for (auto& g : p->seg)
+    if (g.n_tiles) {
+      need = std::max(need, layout_for(g.n_tiles, g.v).total);
+      p->n_tiles += g.n_tiles;
+    }
+  satgb_status st = ensure_ws(p->ws, need, s);
+  if (st != SATGB_OK) return st;
+  cudaError_t e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? SATGB_OK : cuda_fail(e, "cudaStreamSynchronize");
+}
+
+satgb_status plan_launch_locked(satgb_batch_plan_s* p, cudaStream_t s) {
+  for (auto& g : p->seg) {
+    if (!g.n_tiles) continue;
+    satgb_status st = launch_locked(g.v, g.table, g.img0, g.n_images, g.n_tiles, p->ws, p->dev, s, g.order);
+    if (st != SATGB_OK) return st;
+  }
+  return SATGB_OK;
+}
+
+// Captures the classes' launches, one after the other, in the plan's graph.
+satgb_status plan_capture(satgb_batch_plan_s* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+  cudaStream_t cs;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+  satgb_status st = SATGB_OK;
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    const long long before = g_launches.load();
+    st = plan_launch_locked(p, cs);
+    g_launches.store(before); // the capture itself launches nothing
+    cudaError_t e2 = cudaStreamEndCapture(cs, &p->graph);
+    if (st == SATGB_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaStreamEndCapture");
+    if (st == SATGB_OK) {
+      e2 = cudaGraphInstantiate(&p->exec, p->graph, 0);
+      if (e2 != cudaSuccess) st = cuda_fail(e2, "cudaGraphInstantiate");
+    }
+  } else {
+    st = cuda_fail(e, "cudaStreamBeginCapture");
+  }
+  cudaStreamDestroy(cs);
+  return st;
+}
+
+void plan_free(satgb_batch_plan_s* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  ws_free(p->ws.base);
+  for (auto& g : p->seg) seg_free(g);
+  delete p;
+}
+
+}  // namespace
+
+extern "C" {
+
 satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, satgb_dtype out_t, int mode,
                                      int direction, const satgb_image* images, int64_t n_images,
                                      satgb_stream stream) {
@@ -861,18 +1062,11 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   cudaStream_t s = (cudaStream_t)stream;
   // Validate every image; empty images are dropped from the table.
   std::vector<ImgCheck> keep;
-  long long max_w = 0, max_h = 0;
-  double sum_px = 0;
   for (int64_t i = 0; i < n_images; ++i) {
     ImgCheck c{images[i].d_in, images[i].d_out, images[i].in_pitch, images[i].out_pitch, images[i].width, images[i].height};
     satgb_status st = validate_image(c, in_sz, out_sz);
     if (st != SATGB_OK) return fail(st, "image %lld: %s", (long long)i, g_last_error.c_str());
-    if (c.width > 0 && c.height > 0) {
-      keep.push_back(c);
-      max_w = std::max(max_w, c.width);
-      max_h = std::max(max_h, c.height);
-      sum_px += (double)c.width * (double)c.height;
-    }
+    if (c.width > 0 && c.height > 0) keep.push_back(c);
   }
   {
     satgb_status st = check_batch_disjoint(keep, in_sz, out_sz);
@@ -883,83 +1077,97 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   satgb_status st = get_device(&dev);
   if (st != SATGB_OK) return st;
   auto* p = new satgb_batch_plan_s();
+  p->in_t = in_t;
+  p->out_t = out_t;
+  p->mode = mode;
+  p->dir = direction;
   p->dev = dev;
-  // configuration: the tuning entry of the mean image size, else the heuristic
-  const long long side = (long long)std::sqrt(std::max(1.0, sum_px / std::max<size_t>(1, keep.size())));
-  int cfg = g_forced_config >= 0 ? g_forced_config : -1;
-  if (cfg < 0) {
-    tune_load_locked();
-    auto it = g_tune.find(TuneKey(in_t, out_t, mode, direction, log2_bucket(side), log2_bucket(side), sms_of(dev)));
-    // untuned: the 64-row two-CTA tiles waste the least on small and uneven
-    // images; f64 outputs keep the warp-specialized tiles
-    cfg = it != g_tune.end() ? it->second : (dtype_size((satgb_dtype)out_t) == 8 ? 0 : 2);
-  }
-  p->v = find_variant(in_t, out_t, mode, direction, cfg);
-  if (!p->v) p->v = find_variant(in_t, out_t, mode, direction, 0);
-  std::vector<ImageDesc> table;
-  long long base = 0;
+  const int cpt = (int)(16 / out_sz);
   for (auto& c : keep) {
-    ImageDesc d;
-    fill_image_desc(d, p->v, in_t, out_t, c.in, c.out, c.in_pitch, c.out_pitch, c.width, c.height, base, 1, 0, 0);
-    base += (long long)d.ntx * d.nty;
-    table.push_back(d);
+    const long long tiles = ((c.width + 32LL * cpt - 1) / (32LL * cpt)) * ((c.height + 127) / 128);
+    BatchSeg& g = p->seg[tiles >= kLargeTiles ? 0 : 1];
+    g.imgs.push_back(c);
+    g.n_images += 1;
+    g.pixels += (double)c.width * (double)c.height;
+    p->all_tma = p->all_tma && ((uintptr_t)c.in % 16) == 0 && ((uintptr_t)c.out % 16) == 0 &&
+                 ((size_t)c.in_pitch * in_sz) % 16 == 0 && ((size_t)c.out_pitch * out_sz) % 16 == 0;
   }
-  p->n_images = (long long)table.size();
-  p->n_tiles = base;
-  if (!table.empty()) {
-    p->img0 = table[0];
-    if (cudaMalloc(&p->table, table.size() * sizeof(ImageDesc)) != cudaSuccess) {
-      cudaGetLastError();
-      delete p;
-      return fail(SATGB_ERR_ALLOC, "image table allocation failed");
+  tune_load_locked();
+  const int sms = sms_of(dev);
+  for (int cls = 0; cls < kBatchClasses && st == SATGB_OK; ++cls) {
+    if (!p->seg[cls].n_images) continue;
+    int cfg = g_forced_config;
+    if (cfg < 0) {
+      auto it = g_batch_tune.find(batch_key(p, cls, sms));
+      cfg = it != g_batch_tune.end() ? it->second : batch_default_config(p, cls);
     }
-    cudaError_t e = cudaMemcpyAsync(p->table, table.data(), table.size() * sizeof(ImageDesc), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) {
-      cudaFree(p->table);
-      delete p;
-      return cuda_fail(e, "image table upload");
-    }
-    st = ensure_ws(p->ws, layout_for(p->n_tiles, p->v).total, s);
-    if (st == SATGB_OK) {
-      e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize");
-    }
-    if (st == SATGB_OK) {
-      // capture the launch into a graph on a private stream
-      cudaStream_t cs;
-      e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-      if (e == cudaSuccess) {
-        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-          const long long before = g_launches.load();
-          st = launch_locked(p->v, p->table, p->img0, p->n_images, p->n_tiles, p->ws, dev, cs);
-          g_launches.store(before); // the capture itself launches nothing
-          cudaError_t e2 = cudaStreamEndCapture(cs, &p->graph);
-          if (st == SATGB_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaStreamEndCapture");
-          if (st == SATGB_OK) {
-            e2 = cudaGraphInstantiate(&p->exec, p->graph, 0);
-            if (e2 != cudaSuccess) st = cuda_fail(e2, "cudaGraphInstantiate");
-          }
-        } else {
-          st = cuda_fail(e, "cudaStreamBeginCapture");
-        }
-        cudaStreamDestroy(cs);
-      } else {
-        st = cuda_fail(e, "cudaStreamCreate");
-      }
-    }
-    if (st != SATGB_OK) {
-      if (p->exec) cudaGraphExecDestroy(p->exec);
-      if (p->graph) cudaGraphDestroy(p->graph);
-      ws_free(p->ws.base);
-      cudaFree(p->table);
-      delete p;
-      return st;
-    }
+    st = seg_build(p, cls, cfg, s);
+  }
+  if (st == SATGB_OK) st = plan_ws(p, s);
+  if (st == SATGB_OK && p->n_tiles > 0) st = plan_capture(p);
+  if (st != SATGB_OK) {
+    plan_free(p);
+    return st;
   }
   *plan = p;
   return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_autotune(satgb_batch_plan* p, satgb_stream stream, int* configs) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  cudaStream_t s = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> lk(g_mu);
+  tune_load_locked();
+  const int sms = sms_of(p->dev);
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return cuda_fail(cudaGetLastError(), "cudaEventCreate");
+  satgb_status st = SATGB_OK;
+  for (int cls = 0; cls < kBatchClasses && st == SATGB_OK; ++cls) {
+    BatchSeg& g = p->seg[cls];
+    if (configs) configs[cls] = -1;
+    if (!g.n_images) continue;
+    int best = -1;
+    float best_ms = 1e30f;
+    for (int cfg = 0; cfg < kNumConfigs && st == SATGB_OK; ++cfg) {
+      const Variant* v = find_variant(p->in_t, p->out_t, p->mode, p->dir, cfg);
+      if (!v || v->cfg != cfg) continue;
+      st = seg_build(p, cls, cfg, s);
+      if (st == SATGB_OK) st = plan_ws(p, s);
+      if (st != SATGB_OK) break;
+      for (int i = 0; i < 2 && st == SATGB_OK; ++i)
+        st = launch_locked(g.v, g.table, g.img0, g.n_images, g.n_tiles, p->ws, p->dev, s, g.order);
+      const int reps = 5;
+      cudaEventRecord(e0, s);
+      for (int i = 0; i < reps && st == SATGB_OK; ++i)
+        st = launch_locked(g.v, g.table, g.img0, g.n_images, g.n_tiles, p->ws, p->dev, s, g.order);
+      cudaEventRecord(e1, s);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) st = cuda_fail(e, "cudaEventSynchronize");
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (st == SATGB_OK && ms < best_ms) {
+        best_ms = ms;
+        best = cfg;
+      }
+    }
+    if (st != SATGB_OK) break;
+    st = seg_build(p, cls, best, s);
+    g_batch_tune[batch_key(p, cls, sms)] = best;
+    if (configs) configs[cls] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == SATGB_OK) st = plan_ws(p, s);
+  if (st == SATGB_OK) {
+    WsHeader h;
+    cudaError_t e = cudaMemcpy(&h, p->ws.base, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpy");
+    else if (h.sticky) st = fail(SATGB_ERR_TIMEOUT, "a look-back wait timed out while tuning (tile %u)", h.sticky_tile);
+  }
+  if (st == SATGB_OK) tune_save_locked();
+  if (st == SATGB_OK && p->n_tiles > 0) st = plan_capture(p);
+  return st;
 }
 
 satgb_status satgb_batch_plan_exec(satgb_batch_plan* p, satgb_stream stream) {
@@ -967,7 +1175,8 @@ satgb_status satgb_batch_plan_exec(satgb_batch_plan* p, satgb_stream stream) {
   if (p->n_tiles == 0) return SATGB_OK;
   cudaError_t e = cudaGraphLaunch(p->exec, (cudaStream_t)stream);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
-  g_launches.fetch_add(1);
+  for (auto& g : p->seg)
+    if (g.n_tiles) g_launches.fetch_add(1);
   return SATGB_OK;
 }
 
@@ -975,13 +1184,27 @@ satgb_status satgb_batch_plan_launch(satgb_batch_plan* p, satgb_stream stream) {
   if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
   if (p->n_tiles == 0) return SATGB_OK;
   std::lock_guard<std::mutex> lk(g_mu);
-  return launch_locked(p->v, p->table, p->img0, p->n_images, p->n_tiles, p->ws, p->dev, (cudaStream_t)stream);
+  return plan_launch_locked(p, (cudaStream_t)stream);
 }
 
 satgb_status satgb_batch_plan_info(const satgb_batch_plan* p, int64_t* n_tiles, int* config) {
   if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
   if (n_tiles) *n_tiles = p->n_tiles;
-  if (config) *config = p->v ? p->v->cfg : -1;
+  if (config) {
+    // the configuration of the large class, or of the small one if it is alone
+    *config = p->seg[0].n_images ? p->seg[0].v->cfg : (p->seg[1].n_images ? p->seg[1].v->cfg : -1);
+  }
+  return SATGB_OK;
+}
+
+satgb_status satgb_batch_plan_classes(const satgb_batch_plan* p, int64_t* n_images, int64_t* n_tiles, int* configs) {
+  if (!p) return fail(SATGB_ERR_INVALID_ARG, "null plan");
+  for (int cls = 0; cls < kBatchClasses; ++cls) {
+    const BatchSeg& g = p->seg[cls];
+    if (n_images) n_images[cls] = g.n_images;
+    if (n_tiles) n_tiles[cls] = g.n_tiles;
+    if (configs) configs[cls] = g.n_images ? g.v->cfg : -1;
+  }
   return SATGB_OK;
 }
 
@@ -1004,11 +1227,7 @@ satgb_status satgb_batch_plan_check(satgb_batch_plan* p, satgb_stream stream) {
 satgb_status satgb_batch_plan_destroy(satgb_batch_plan* p) {
   if (!p) return SATGB_OK;
   cudaDeviceSynchronize();
-  if (p->exec) cudaGraphExecDestroy(p->exec);
-  if (p->graph) cudaGraphDestroy(p->graph);
-  ws_free(p->ws.base);
-  if (p->table) cudaFree(p->table);
-  delete p;
+  plan_free(p);
   return SATGB_OK;
 }
 

@@ -564,19 +564,26 @@ def test_scans_pitched_and_full_size(cuda, oracle):
 @pytest.mark.parametrize("pitched", [True, False])
 def test_batch512_bit_exact(cuda, oracle, pitched):
     """The batch workload exactly as the bench builds it: 512 u8 images with
-    widths and heights log-uniform in [64, 4096] (about 590 M pixels, 78,000
-    tiles), rows pitched to 128 bytes or packed, one graph replay of the plan;
-    every image bit-exact against the oracle."""
+    widths and heights log-uniform in [64, 4096] (about 590 M pixels), rows
+    pitched to 128 bytes or packed, one graph replay of the plan with its
+    untuned configurations and one after the batch autotuner picked a
+    configuration per size class; every image bit-exact against the oracle."""
     from bench import build_batch
     xs, ys, _ = build_batch(cuda, pitched=pitched)
     plan = sat_gb300.BatchPlan(xs, ys)
-    for y in ys:
-        y.view(torch.int32).fill_(-1)
-    plan.exec()
-    plan.check()
-    for i, (x, y) in enumerate(zip(xs, ys)):
-        a = to_np(x)
-        assert np.array_equal(bits(to_np(y)), bits(oracle.sat_serial(a, np.uint32))), i
+    cls = plan.classes()
+    assert cls[0]["images"] > 0 and cls[1]["images"] > 0 and cls[0]["images"] + cls[1]["images"] == 512
+    for rep, tuned in ((0, False), (1, True)):
+        if tuned:
+            chosen = plan.autotune()  # every configuration of each class, timed on these images
+            assert [c["config"] for c in plan.classes()] == list(chosen)
+        for y in ys:
+            y.view(torch.int32).fill_(-1)
+        plan.exec()
+        plan.check()
+        for i, (x, y) in enumerate(zip(xs, ys)):
+            a = to_np(x)
+            assert np.array_equal(bits(to_np(y)), bits(oracle.sat_serial(a, np.uint32))), (tuned, i)
     plan.close()
 
 
