@@ -898,9 +898,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       A rs = AR::zero();
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
-        const A a = Cvt<A, TIn>::in(x.u.e[c]);
-        colp[c] = AR::add(colp[c], a);
-        rs = AR::add(rs, a);
+        colp[c] = AddIn<A, TIn>::add(colp[c], x.u.e[c]);
+        rs = AddIn<A, TIn>::add(rs, x.u.e[c]);
       }
       rowp[r] = rs;
     }

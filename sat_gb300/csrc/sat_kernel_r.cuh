@@ -170,9 +170,8 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel_r(const __grid_
       A rs = AR::zero();
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
-        const A a = Cvt<A, TIn>::in(x[r].u.e[c]);
-        colp[c] = AR::add(colp[c], a);
-        rs = AR::add(rs, a);
+        colp[c] = AddIn<A, TIn>::add(colp[c], x[r].u.e[c]);
+        rs = AddIn<A, TIn>::add(rs, x[r].u.e[c]);
       }
       rowp[r] = rs;
     }
@@ -337,7 +336,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel_r(const __grid_
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
-          run = AR::add(run, Cvt<A, TIn>::in(x[r].u.e[c]));
+          run = AddIn<A, TIn>::add(run, x[r].u.e[c]);
           top[c] = AR::add(top[c], run);
           o.e[c] = OutCvt<TOut, A>::out(top[c]);
         }

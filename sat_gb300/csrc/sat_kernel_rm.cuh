@@ -233,9 +233,8 @@ __global__ void __launch_bounds__(TileShapeRM<TIn, TOut, A, RPW, NWC>::THREADS, 
         A rs = AR::zero();
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-          const A a = Cvt<A, TIn>::in(x.u.e[c]);
-          colp[c] = AR::add(colp[c], a);
-          rs = AR::add(rs, a);
+          colp[c] = AddIn<A, TIn>::add(colp[c], x.u.e[c]);
+          rs = AddIn<A, TIn>::add(rs, x.u.e[c]);
         }
         rowp[r] = rs;
       }
@@ -332,7 +331,7 @@ __global__ void __launch_bounds__(TileShapeRM<TIn, TOut, A, RPW, NWC>::THREADS, 
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
-          run = AR::add(run, Cvt<A, TIn>::in(xin[r].u.e[c]));
+          run = AddIn<A, TIn>::add(run, xin[r].u.e[c]);
           top[c] = AR::add(top[c], run);
           o[c] = OutCvt<TOut, A>::out(top[c]);
         }

@@ -254,9 +254,8 @@ __global__ void __launch_bounds__(TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CT
         A rs = AR::zero();
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-          const A a = Cvt<A, TIn>::in(x.u.e[c]);
-          colp[c] = AR::add(colp[c], a);
-          rs = AR::add(rs, a);
+          colp[c] = AddIn<A, TIn>::add(colp[c], x.u.e[c]);
+          rs = AddIn<A, TIn>::add(rs, x.u.e[c]);
         }
         rowp[r] = rs;
       }
@@ -357,7 +356,7 @@ __global__ void __launch_bounds__(TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CT
 #pragma unroll
           for (int ii = 0; ii < CPT; ++ii) {
             const int c = REV ? CPT - 1 - ii : ii;
-            run = AR::add(run, Cvt<A, TIn>::in(xin[r].u.e[c]));
+            run = AddIn<A, TIn>::add(run, xin[r].u.e[c]);
             top[c] = AR::add(top[c], run);
             o[c] = OutCvt<TOut, A>::out(top[c]);
           }
@@ -390,7 +389,7 @@ __global__ void __launch_bounds__(TileShapeWS<TIn, TOut, A, RPW, NWC, DIRECT, CT
 #pragma unroll
         for (int ii = 0; ii < CPT; ++ii) {
           const int c = REV ? CPT - 1 - ii : ii;
-          run = AR::add(run, Cvt<A, TIn>::in(x.u.e[c]));
+          run = AddIn<A, TIn>::add(run, x.u.e[c]);
           top[c] = AR::add(top[c], run);
           o.e[c] = OutCvt<TOut, A>::out(top[c]);
         }

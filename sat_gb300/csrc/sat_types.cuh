@@ -126,6 +126,22 @@ struct Cvt<CF32, TIn> {
   __device__ __forceinline__ static CF32 in(TIn x) { return CF32{(float)x, 0.f}; }
 };
 
+// acc + one input element.  The compensated accumulator's element carries no
+// error term, so a TwoSum of the sums and one add of the errors do: one add
+// fewer per element than the general pair + pair addition.
+template <class A, class TIn>
+struct AddIn {
+  __device__ __forceinline__ static A add(A acc, TIn x) { return Ar<A>::add(acc, Cvt<A, TIn>::in(x)); }
+};
+template <class TIn>
+struct AddIn<CF32, TIn> {
+  __device__ __forceinline__ static CF32 add(CF32 acc, TIn x) {
+    float err;
+    const float s = two_sum(acc.s, (float)x, err);
+    return CF32{s, __fadd_rn(acc.e, err)};
+  }
+};
+
 template <class TOut, class A>
 struct OutCvt;
 template <>
