@@ -252,6 +252,7 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         sub.update(stress_result(dev, stream, peak))
         torch.cuda.empty_cache()
+        sub["reference_gpu_8192"] = reference_gpu_result()
 
     # ---- e2e: the same headline SAT through the public API with host buffers ----
     # Every step copies its input from pinned host memory, runs the SAT and
@@ -585,6 +586,34 @@ def box_result(dev, stream):
     sat_bytes = x.numel() * 8
     return {"shape": list(x.shape), "radii": list(radii), "fwd_ms": round(f, 4), "fwd_bwd_ms": round(fb, 4),
             "fwd_bwd_over_fwd": round(fb / f, 3), "forward_sat_bytes": int(sat_bytes)}
+
+
+def reference_gpu_result(size=8192, reps=20):
+    """The reference's own GPU kernels (its three two-launch algorithms, built
+    from its sources for sm_103a by baseline/build_ref_gpu.sh into
+    baseline/_ref/*.cubin) timed on this GPU by baseline/ref_gpu_bench.cu
+    with the reference's launch shapes, each result checked on the host.
+    Reported beside this library's figures; never part of the library."""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    cubins = ("ScanRow-BRLT.cubin", "BRLT-Scan.cubin", "ScanRowColumn.cubin")
+    if not all(os.path.isfile(os.path.join(ref, c)) for c in cubins):
+        return {"unavailable": "the reference's kernels were not built here (baseline/build_ref_gpu.sh needs the "
+                               "reference sources)"}
+    exe = os.path.join(ref, "ref_gpu_bench")
+    src = os.path.join(ROOT, "baseline", "ref_gpu_bench.cu")
+    from sat_gb300 import build as B
+    r = subprocess.run([B.nvcc_path(), "-O2", "-std=c++17", "-o", exe, src, "-lcuda"], capture_output=True, text=True)
+    if r.returncode != 0:
+        return {"unavailable": "harness build failed: " + r.stderr.strip().splitlines()[-1] if r.stderr else "?"}
+    r = subprocess.run([exe, ref, str(size), str(reps)], capture_output=True, text=True, timeout=600)
+    if r.returncode != 0:
+        return {"unavailable": "harness failed: " + (r.stderr.strip().splitlines() or ["?"])[-1]}
+    res = {}
+    for line in r.stdout.splitlines():
+        if line.startswith("{"):
+            d = json.loads(line)
+            res[f"{d['algorithm']} {d['pair']}"] = {k: d[k] for k in ("ms_median", "gbs", "correct", "launches")}
+    return res
 
 
 def stress_result(dev, stream, peak):
