@@ -680,7 +680,8 @@ def run_workload(args):
         sat_gb300.stream_check()
         print(json.dumps({"case": args.case, "n": n, "ms_median": round(statistics.median(per), 5)}))
     elif args.case == "box_parts":
-        # the four launches of the box-filter layer's forward + backward, each timed alone
+        # the four launches of the box-filter layer's forward + backward, each timed alone, and the
+        # one-call backward (adjoint into the output, reverse SAT in place) that makes the last two
         from sat_gb300 import api
         n = 8 if args.small else 64
         x, wts, radii = build_box(dev, n=n)
@@ -689,10 +690,11 @@ def run_workload(args):
         parts = {"sat": lambda: api.sat(x, torch.float32, out=s),
                  "box_means": lambda: api.box_means_from_sat(s, radii),
                  "adjoint": lambda: api.box_means_adjoint(wts, radii, out=gs),
-                 "reverse_sat": lambda: api.sat(gs, torch.float32, reverse=True, out=gs)}
+                 "reverse_sat": lambda: api.sat(gs, torch.float32, reverse=True, out=gs),
+                 "grad_x": lambda: api.box_means_grad_x(wts, radii, out=gs)}
         plane = x.numel() * 4
         moved = {"sat": 2 * plane, "box_means": (1 + len(radii)) * plane, "adjoint": (len(radii) + 1) * plane,
-                 "reverse_sat": 2 * plane}
+                 "reverse_sat": 2 * plane, "grad_x": (len(radii) + 3) * plane}
         res = {"case": args.case, "n": n}
         for name, fn in parts.items():
             _, per = _time_steps(fn, args.steps, args.warmup, stream, 0.0)

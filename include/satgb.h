@@ -195,6 +195,14 @@ satgb_status satgb_box_filter_fwd(const satgb_box_desc* desc, satgb_stream strea
  * radii's means (the four-corner scatter, computed as a gather so it is
  * deterministic).  d_sat is overwritten. */
 satgb_status satgb_box_filter_bwd(const satgb_box_desc* desc, satgb_stream stream);
+/* The gradient of the box means with respect to the image the SAT was taken
+ * of, dL/dx = reverse SAT of dL/dSAT, in one call and without scratch memory:
+ * dL/dSAT is gathered into d_dx, then d_dx is reverse-summed in place (two
+ * tile launches and the edge launch of satgb_box_filter_bwd).  desc->d_sat is
+ * not used; d_dx (n_planes planes of width x height, pitch and plane stride in
+ * elements) is written and may not overlap the gradients of the means. */
+satgb_status satgb_box_filter_bwd_x(const satgb_box_desc* desc, void* d_dx, int64_t dx_pitch,
+                                    int64_t dx_plane_stride, satgb_stream stream);
 
 /* The same single-image SAT as satgb_sat_ex, for callers that cannot allocate
  * device memory: code running inside an allocator or memory-pool callback, in

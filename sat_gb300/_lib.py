@@ -109,6 +109,7 @@ SIGNATURES = {
     "satgb_scan_cols": (_ST, [_I, _I, _P, _I64, _P, _I64, _I64, _I64, _P]),
     "satgb_box_filter_fwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),
     "satgb_box_filter_bwd": (_ST, [ctypes.POINTER(satgb_box_desc), _P]),
+    "satgb_box_filter_bwd_x": (_ST, [ctypes.POINTER(satgb_box_desc), _P, _I64, _I64, _P]),
 }
 
 _lib = None

@@ -261,6 +261,23 @@ def box_means_adjoint(grad_boxes: torch.Tensor, radii: Sequence[int], out=None, 
     return out
 
 
+def box_means_grad_x(grad_boxes: torch.Tensor, radii: Sequence[int], out=None, stream=None) -> torch.Tensor:
+    """dL/dx of the box means of x from dL/dmeans (..., R, H, W) in one call:
+    the adjoint gather writes dL/dSAT into out, which is then reverse-summed
+    in place (no scratch tensor)."""
+    shape = grad_boxes.shape[:-3] + grad_boxes.shape[-2:]
+    if out is None:
+        out = torch.empty(shape, dtype=torch.float32, device=grad_boxes.device)
+    elif out.shape != shape or out.dtype != torch.float32:
+        raise SatError(_lib.ERR_INVALID_ARG, "out must be an f32 (..., H, W) tensor")
+    d = _box_desc(out, grad_boxes, radii)
+    o3 = out if out.dim() >= 3 else out.unsqueeze(0)
+    _, opitch, _, _, _, oplane = _planes_args(o3)
+    d.d_sat = None
+    check(_lib.load().satgb_box_filter_bwd_x(ctypes.byref(d), out.data_ptr(), opitch, oplane, _stream_handle(stream)))
+    return out
+
+
 def stream_check(stream=None) -> None:
     """Synchronises the stream and raises SatError(SATGB_ERR_TIMEOUT) when a
     look-back wait of an earlier call gave up."""

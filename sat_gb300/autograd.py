@@ -8,8 +8,9 @@ the incoming gradient, one launch of the same kernel with direction=reverse.
 
 Box filter.  box_filter_means(x, radii) returns the clipped box means of every
 radius, read by four corners from the SAT of x (one SAT launch plus one box
-launch forward; one adjoint-gather launch plus one reverse-SAT launch
-backward).
+launch forward).  Backward: the adjoint gather into the gradient tensor,
+then the reverse SAT of that tensor in place (the plain mode in one call of
+the library, the compensated mode with the compensated reverse SAT).
 """
 from __future__ import annotations
 
@@ -65,6 +66,9 @@ class BoxMeansFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g: torch.Tensor):
         g = _as_f32_cuda(g)
+        if ctx.mode == "plain":
+            # adjoint gather and in-place reverse SAT in one library call
+            return api.box_means_grad_x(g, ctx.radii), None, None
         gs = api.box_means_adjoint(g, ctx.radii)
         # the reverse SAT may overwrite its input in place: gs is ours alone
         return api.sat(gs, torch.float32, mode=ctx.mode, reverse=True, out=gs), None, None

@@ -881,6 +881,43 @@ satgb_status satgb_autotune(satgb_dtype in_t, satgb_dtype out_t, int mode, const
 }
 
 // ---------------------------------------------------------------------------
+// box-filter backward to the image
+// ---------------------------------------------------------------------------
+satgb_status satgb_box_filter_bwd_x(const satgb_box_desc* desc, void* d_dx, int64_t dx_pitch,
+                                    int64_t dx_plane_stride, satgb_stream stream) {
+  if (!desc) return fail(SATGB_ERR_INVALID_ARG, "box filter backward: null descriptor");
+  const long long w = desc->width, h = desc->height, planes = desc->n_planes;
+  if (w < 0 || h < 0 || planes < 0 || desc->n_radii < 1 || desc->n_radii > SATGB_MAX_RADII)
+    return fail(SATGB_ERR_INVALID_ARG, "box filter backward: invalid sizes or radius count");
+  if (w == 0 || h == 0 || planes == 0) return SATGB_OK;
+  if (!d_dx) return fail(SATGB_ERR_INVALID_ARG, "box filter backward: null gradient output");
+  if (((uintptr_t)d_dx % 4) != 0) return fail(SATGB_ERR_MISALIGNED, "box filter backward: f32 pointer not 4-byte aligned");
+  const long long span = (h - 1) * dx_pitch + w;
+  if (dx_pitch < w || (planes > 1 && dx_plane_stride < span))
+    return fail(SATGB_ERR_INVALID_ARG, "box filter backward: gradient output pitch or plane stride too small");
+  // the output may not overlap any gradient plane it is computed from
+  if (desc->box_pitch >= w && (planes == 1 || desc->box_plane_stride > 0)) {
+    const long long gspan = ((h - 1) * desc->box_pitch + w) + (planes - 1) * (planes > 1 ? desc->box_plane_stride : 0);
+    const long long xspan = span + (planes - 1) * (planes > 1 ? dx_plane_stride : 0);
+    const char* xb = (const char*)d_dx;
+    for (int i = 0; i < desc->n_radii; ++i) {
+      const char* gb = (const char*)desc->d_box[i];
+      if (gb && xb < gb + gspan * 4 && gb < xb + xspan * 4)
+        return fail(SATGB_ERR_INVALID_ARG, "box filter backward: the gradient output overlaps the gradients of the means");
+    }
+  }
+  // dL/dSAT into the output, then its reverse SAT in place
+  satgb_box_desc d = *desc;
+  d.d_sat = d_dx;
+  d.sat_pitch = dx_pitch;
+  d.sat_plane_stride = planes > 1 ? dx_plane_stride : 0;
+  satgb_status st = satgb_box_filter_bwd(&d, stream);
+  if (st != SATGB_OK) return st;
+  return sat_single(SATGB_F32, SATGB_F32, SATGB_MODE_PLAIN, SATGB_REVERSE, d_dx, dx_pitch, d_dx, dx_pitch, w, h,
+                    (cudaStream_t)stream, -1, planes, d.sat_plane_stride, d.sat_plane_stride);
+}
+
+// ---------------------------------------------------------------------------
 // batch plans
 // ---------------------------------------------------------------------------
 }  // extern "C"

@@ -111,6 +111,27 @@ def test_box_filter_validation(satlib):
         assert call(w=0) == _lib.OK and call(h=0) == _lib.OK and call(planes=0) == _lib.OK
 
 
+def test_box_grad_x_validation(satlib):
+    """satgb_box_filter_bwd_x checks its descriptor like the other box-filter
+    calls (the SAT buffer is not needed), then its output: present, aligned,
+    pitch and plane stride large enough, no overlap with the gradients read."""
+    d = _lib.satgb_box_desc()
+    d.width, d.height, d.n_planes = 64, 64, 1
+    d.n_radii = 1
+    d.radius[0] = 3
+    d.d_box[0] = 0x200000
+    d.box_pitch, d.box_plane_stride = 64, 64 * 64
+    f = satlib.satgb_box_filter_bwd_x
+    assert f(ctypes.byref(d), None, 64, 64 * 64, None) == _lib.ERR_INVALID_ARG
+    assert f(ctypes.byref(d), 0x300002, 64, 64 * 64, None) == _lib.ERR_MISALIGNED
+    assert f(ctypes.byref(d), 0x300000, 63, 64 * 64, None) == _lib.ERR_INVALID_ARG
+    assert f(ctypes.byref(d), 0x200000 + 4 * 100, 64, 64 * 64, None) == _lib.ERR_INVALID_ARG  # overlaps g
+    d.n_radii = 0
+    assert f(ctypes.byref(d), 0x300000, 64, 64 * 64, None) == _lib.ERR_INVALID_ARG
+    d.n_radii, d.width = 1, 0
+    assert f(ctypes.byref(d), 0x300000, 64, 64 * 64, None) == _lib.OK  # empty: nothing to do
+
+
 def test_error_string_set_on_failure(satlib):
     assert _call(satlib, "satgb_scanrow_brlt", _lib.U8, _lib.U32, w=-1) == _lib.ERR_INVALID_ARG
     assert b"width" in satlib.satgb_last_error_string()

@@ -283,3 +283,37 @@ def test_box_filter_rejects_bad_args(cuda):
         api.box_means_from_sat(s, (-1,))
     with pytest.raises(sat_gb300.SatError):
         api.box_means_from_sat(s.double(), (1,))
+
+
+@pytest.mark.parametrize("shape,radii", [((2, 3, 256, 256), (3, 7, 15)), ((1, 2, 200, 333), (2, 9, 32)),
+                                         ((1, 1, 97, 131), (0, 1, 32, 70)), ((3, 1, 1, 9), (1,)),
+                                         ((2, 1, 1, 1), (0, 3)), ((1, 2, 300, 1), (4,)),
+                                         ((1, 1, 129, 257), (1, 128))])
+def test_grad_x_matches_separate_calls(cuda, shape, radii):
+    """satgb_box_filter_bwd_x (adjoint gather into the output, reverse SAT in
+    place) against the separate calls (adjoint into a dL/dSAT tensor, then the
+    reverse SAT into a new tensor): to 1e-5 of the largest gradient, and both
+    to the float64 autograd gradient."""
+    g = torch.Generator(device="cpu").manual_seed(27)
+    wts = torch.randn(shape[:-2] + (len(radii),) + shape[-2:], generator=g).to(cuda)
+    gx = api.box_means_grad_x(wts, radii)
+    two = sat_gb300.sat(api.box_means_adjoint(wts, radii), torch.float32, reverse=True)
+    scale = max(1.0, float(two.abs().max()))
+    assert float((gx - two).abs().max()) <= 1e-5 * scale
+    x = torch.randn(shape, generator=g).to(cuda)
+    x64 = x.double().clone().requires_grad_(True)
+    (box_means64(x64, radii) * wts.double()).sum().backward()
+    assert float((gx.double() - x64.grad).abs().max()) <= 1e-4 * max(1.0, float(x64.grad.abs().max()))
+
+
+def test_grad_x_pitched_planes(cuda):
+    """Gradient planes and the output as strided views (row pitch > width)."""
+    g = torch.Generator(device="cpu").manual_seed(28)
+    base = torch.randn((2, 2, 70, 96), generator=g).to(cuda)
+    wts = base[..., :90]
+    out_base = torch.full((2, 70, 100), float("nan"), device=cuda)
+    out = out_base[..., :90]
+    api.box_means_grad_x(wts, (2, 5), out=out)
+    ref = sat_gb300.sat(api.box_means_adjoint(wts.contiguous(), (2, 5)), torch.float32, reverse=True)
+    assert float((out - ref).abs().max()) <= 1e-5 * max(1.0, float(ref.abs().max()))
+    assert bool(torch.isnan(out_base[..., 90:]).all())  # the row padding is never written
