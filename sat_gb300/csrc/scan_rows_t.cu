@@ -6,17 +6,24 @@
 // serielScan launch reads rows and stores the scanned rows transposed
 // (compared there with IntegralImageAllRow + Transpose).  Rows are
 // independent, so there is no look-back: a CTA owns a strip of 32 rows and
-// walks it left to right in tiles of 128 columns.  Warp w (of 16) owns strip rows
-// [2w, 2w+2) and keeps their running sums (the carry) in registers from tile to
-// tile; lane l owns columns [4l, 4l+4) of the tile.  Per tile: in-thread prefix,
-// Kogge-Stone warp scan of the lane totals, plus the carry; the 32 x 128 block
-// of results is transposed through shared memory (row stride 33) and leaves as
-// 128 output rows of 32 consecutive elements, one coalesced store per warp and
-// row.  The next tile's inputs are loaded before the current one is scanned.
+// walks it left to right in tiles of 32 x CPT columns, CPT = 16 / sizeof(in),
+// so that every thread reads one 16-byte vector per row and tile whatever the
+// input type (a tile is 16 KB of input).  Warp w (of 16) owns strip rows
+// [2w, 2w+2) and keeps their running sums (the carry) in registers from tile
+// to tile; lane l owns columns [l CPT, (l+1) CPT) of the tile.  The next two
+// tiles' vectors are in flight while a tile is scanned (32 KB a CTA), which
+// is what keeps HBM busy with one CTA per 32 rows.  Per tile: in-thread
+// prefix, Kogge-Stone warp scan of the lane totals, plus the carry; the
+// 32-row block of results is transposed through shared memory and leaves as
+// output rows of 32 consecutive elements, one coalesced store per warp and
+// row.  The transpose buffer has rows of 32 with entry y of row x at
+// y ^ ((x / CPT) mod 32): the writes (a lane's CPT columns, fixed y) and the
+// reads (fixed x, y = lane) both touch 32 different banks.
 // Accumulators: u32 for integer outputs (mod-2^32 wrap, i32 results are the
 // two's-complement bits), f32 for f32, f64 for f64.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <type_traits>
 
@@ -33,8 +40,13 @@ namespace {
 constexpr int kWarps = 16;
 constexpr int kRPW = 2;                 // strip rows per warp
 constexpr int kStrip = kWarps * kRPW;   // 32 rows per CTA
-constexpr int kCPT = 4;                 // tile columns per lane
-constexpr int kTileW = 32 * kCPT;       // 128 columns per tile
+constexpr int kMaxTileW = 32 * 16;      // the widest tile (1-byte inputs)
+
+template <class TIn>
+struct Shape {
+  static constexpr int CPT = 16 / (int)sizeof(TIn); // tile columns per lane
+  static constexpr int TW = 32 * CPT;               // tile columns
+};
 
 template <class A, class TIn>
 __device__ __forceinline__ A to_acc(TIn v) {
@@ -51,38 +63,29 @@ __device__ __forceinline__ TOut from_acc(A v) {
   return (TOut)v; // u32 -> i32 keeps the bits
 }
 
-// one vector access for N elements of up to 16 bytes in all
-template <class TIn, int N>
-struct Vec {
-  static_assert(sizeof(TIn) * N <= 16, "at most one 16-byte access");
-  using T = typename std::conditional<sizeof(TIn) * N == 4, uint32_t,
-            typename std::conditional<sizeof(TIn) * N == 8, uint2, uint4>::type>::type;
+template <class TIn>
+union Seg {
+  uint4 u;
+  TIn e[Shape<TIn>::CPT];
 };
 
-// this warp's kRPW rows x kCPT columns of the tile at column x0; zero outside the image
+// this warp's kRPW rows x CPT columns of the tile at column x (raw 16-byte
+// vectors); zero outside the image
 template <class TIn>
 __device__ __forceinline__ void load_tile(const TIn* in, long long pitch, int W, int H, int y, int x, bool vec,
-                                          TIn (&v)[kRPW][kCPT]) {
+                                          uint4 (&v)[kRPW]) {
+  constexpr int CPT = Shape<TIn>::CPT;
 #pragma unroll
   for (int r = 0; r < kRPW; ++r) {
     const TIn* row = in + (long long)(y + r) * pitch;
     const bool yin = y + r < H;
-    bool done = false;
-    if constexpr (sizeof(TIn) * kCPT <= 16) { // 8-byte inputs: two 16-byte halves, element by element below
-      if (vec && yin && x + kCPT <= W) {
-        union {
-          typename Vec<TIn, kCPT>::T u;
-          TIn e[kCPT];
-        } s;
-        s.u = __ldcs(reinterpret_cast<const typename Vec<TIn, kCPT>::T*>(row + x));
+    if (vec && yin && x + CPT <= W) {
+      v[r] = __ldcs(reinterpret_cast<const uint4*>(row + x));
+    } else {
+      Seg<TIn> s;
 #pragma unroll
-        for (int c = 0; c < kCPT; ++c) v[r][c] = s.e[c];
-        done = true;
-      }
-    }
-    if (!done) {
-#pragma unroll
-      for (int c = 0; c < kCPT; ++c) v[r][c] = (yin && x + c < W) ? __ldcs(row + x + c) : TIn(0);
+      for (int c = 0; c < CPT; ++c) s.e[c] = (yin && x + c < W) ? __ldcs(row + x + c) : TIn(0);
+      v[r] = s.u;
     }
   }
 }
@@ -91,7 +94,9 @@ template <class TIn, class TOut, class A>
 __global__ void __launch_bounds__(kWarps * 32) scan_rows_t_kernel(const TIn* __restrict__ in, long long in_pitch,
                                                                   TOut* __restrict__ out, long long out_pitch, int W,
                                                                   int H, bool vec) {
-  __shared__ A tr[kTileW][kStrip + 1];
+  constexpr int CPT = Shape<TIn>::CPT, TW = Shape<TIn>::TW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  A* tr = reinterpret_cast<A*>(smem_raw); // TW rows of 32 (swizzled)
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int y0 = blockIdx.x * kStrip;
@@ -99,22 +104,24 @@ __global__ void __launch_bounds__(kWarps * 32) scan_rows_t_kernel(const TIn* __r
   A carry[kRPW];
 #pragma unroll
   for (int r = 0; r < kRPW; ++r) carry[r] = A(0);
-  TIn nxt[kRPW][kCPT];
-  load_tile<TIn>(in, in_pitch, W, H, yw, lane * kCPT, vec, nxt);
-  for (int x0 = 0; x0 < W; x0 += kTileW) {
-    TIn cur[kRPW][kCPT];
+  uint4 n0[kRPW], n1[kRPW];
+  load_tile<TIn>(in, in_pitch, W, H, yw, lane * CPT, vec, n0);
+  if (TW < W) load_tile<TIn>(in, in_pitch, W, H, yw, TW + lane * CPT, vec, n1);
+  for (int x0 = 0; x0 < W; x0 += TW) {
+    Seg<TIn> cur[kRPW];
 #pragma unroll
-    for (int r = 0; r < kRPW; ++r)
-#pragma unroll
-      for (int c = 0; c < kCPT; ++c) cur[r][c] = nxt[r][c];
-    if (x0 + kTileW < W) load_tile<TIn>(in, in_pitch, W, H, yw, x0 + kTileW + lane * kCPT, vec, nxt);
-    A v[kRPW][kCPT];
+    for (int r = 0; r < kRPW; ++r) {
+      cur[r].u = n0[r];
+      n0[r] = n1[r];
+    }
+    if (x0 + 2 * TW < W) load_tile<TIn>(in, in_pitch, W, H, yw, x0 + 2 * TW + lane * CPT, vec, n1);
+    A v[kRPW][CPT];
     A incl[kRPW];
 #pragma unroll
     for (int r = 0; r < kRPW; ++r) {
 #pragma unroll
-      for (int c = 0; c < kCPT; ++c) v[r][c] = c ? v[r][c - 1] + to_acc<A>(cur[r][c]) : to_acc<A>(cur[r][c]);
-      incl[r] = v[r][kCPT - 1];
+      for (int c = 0; c < CPT; ++c) v[r][c] = c ? v[r][c - 1] + to_acc<A>(cur[r].e[c]) : to_acc<A>(cur[r].e[c]);
+      incl[r] = v[r][CPT - 1];
     }
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -131,30 +138,42 @@ __global__ void __launch_bounds__(kWarps * 32) scan_rows_t_kernel(const TIn* __r
       const A total = __shfl_sync(0xffffffffu, incl[r], 31);
       const A base = carry[r] + ex;
 #pragma unroll
-      for (int c = 0; c < kCPT; ++c) v[r][c] = base + v[r][c];
+      for (int c = 0; c < CPT; ++c) v[r][c] = base + v[r][c];
       carry[r] = carry[r] + total;
     }
     __syncthreads(); // the previous tile's transposed reads are done
+    // column x = lane CPT + c, row y = warp kRPW + r: (x / CPT) mod 32 = lane
 #pragma unroll
     for (int r = 0; r < kRPW; ++r)
 #pragma unroll
-      for (int c = 0; c < kCPT; ++c) tr[lane * kCPT + c][warp * kRPW + r] = v[r][c];
+      for (int c = 0; c < CPT; ++c) tr[(lane * CPT + c) * 32 + ((warp * kRPW + r) ^ lane)] = v[r][c];
     __syncthreads();
     const int y = y0 + lane;
 #pragma unroll 4
-    for (int xr = warp; xr < kTileW; xr += kWarps) {
+    for (int xr = warp; xr < TW; xr += kWarps) {
       const int x = x0 + xr;
-      if (x < W && y < H) __stcs(out + (long long)x * out_pitch + y, from_acc<TOut, A>(tr[xr][lane]));
+      if (x < W && y < H) __stcs(out + (long long)x * out_pitch + y, from_acc<TOut, A>(tr[xr * 32 + (lane ^ ((xr / CPT) & 31))]));
     }
   }
 }
 
 template <class TIn, class TOut, class A>
 cudaError_t launch(const void* in, long long in_pitch, void* out, long long out_pitch, int W, int H, cudaStream_t s) {
-  const bool vec = ((uintptr_t)in % (kCPT * sizeof(TIn))) == 0 && ((size_t)in_pitch * sizeof(TIn)) % (kCPT * sizeof(TIn)) == 0;
+  constexpr int smem = Shape<TIn>::TW * 32 * (int)sizeof(A);
+  // the dynamic shared-memory limit, raised once per device (up to 128 KB, for 1-byte inputs and f64 sums)
+  static std::atomic<int> raised[64];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64 || !raised[dev].load(std::memory_order_acquire)) {
+    e = cudaFuncSetAttribute(&scan_rows_t_kernel<TIn, TOut, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) raised[dev].store(1, std::memory_order_release);
+  }
+  const bool vec = ((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * sizeof(TIn)) % 16 == 0;
   const unsigned grid = (unsigned)((H + kStrip - 1) / kStrip);
-  scan_rows_t_kernel<TIn, TOut, A><<<grid, kWarps * 32, 0, s>>>(static_cast<const TIn*>(in), in_pitch,
-                                                                 static_cast<TOut*>(out), out_pitch, W, H, vec);
+  scan_rows_t_kernel<TIn, TOut, A><<<grid, kWarps * 32, smem, s>>>(static_cast<const TIn*>(in), in_pitch,
+                                                                   static_cast<TOut*>(out), out_pitch, W, H, vec);
   return cudaGetLastError();
 }
 
@@ -186,7 +205,7 @@ extern "C" satgb_status satgb_scan_rows_transposed(satgb_dtype in_t, satgb_dtype
     return satgb::api_fail(SATGB_ERR_INVALID_ARG,
                            "scan_rows_transposed: in pitch below the width or out pitch below the height");
   // column and row indices are ints in the kernel, and the tile loop steps past the last column
-  if (width > (1LL << 31) - 2 * kTileW || height > (1LL << 31) - 2 * kStrip || height - 1 > INT64_MAX / 16 / in_pitch ||
+  if (width > (1LL << 31) - 3 * kMaxTileW || height > (1LL << 31) - 2 * kStrip || height - 1 > INT64_MAX / 16 / in_pitch ||
       width - 1 > INT64_MAX / 16 / out_pitch)
     return satgb::api_fail(SATGB_ERR_OVERFLOW, "scan_rows_transposed: image too large");
   if (((uintptr_t)d_in % si) != 0 || ((uintptr_t)d_out % so) != 0)

@@ -485,7 +485,7 @@ def test_scan_rows_transposed_all_pairs(cuda, oracle):
     Transpose) against the oracle's row scan, transposed: bit-exact for integer
     outputs, floats within the scans' tolerance."""
     for name, (ti, to) in oracle.PAIRS.items():
-        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (33, 129), (129, 257), (517, 769)]):
+        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (33, 129), (129, 257), (517, 769), (37, 1601)]):
             a = oracle.gen(PAIR_KINDS[ti], 3500 + i, shape)
             out = to_np(sat_gb300.scan_rows_transposed(to_dev(a), SCAN_TORCH[np.dtype(to)]))
             assert out.shape == (shape[1], shape[0])
