@@ -241,6 +241,12 @@ def run_gpu(args):
         sub[nm] = {"gbs": round(step_bytes / (statistics.median(per_s) / 1e3) / GB, 1),
                    "ms_median": round(statistics.median(per_s), 4)}
         sub[nm]["frac_of_peak"] = round(sub[nm]["gbs"] / peak, 4)
+    # the transposed row scan of u8 -> u32 (5 bytes a pixel; square, so yb takes the transpose)
+    ms, per_s = _time_steps(lambda: sat_gb300.scan_rows_transposed(xb, torch.uint32, out=yb), 50, 5, stream, 0.2)
+    nm = "scan_rows_transposed_u8_u32_8192"
+    sub[nm] = {"gbs": round(xb.numel() * 5 / (statistics.median(per_s) / 1e3) / GB, 1),
+               "ms_median": round(statistics.median(per_s), 4)}
+    sub[nm]["frac_of_peak"] = round(sub[nm]["gbs"] / peak, 4)
     sat_gb300.stream_check()
     del xb, yb, xd, yd
     if not args.no_extra:

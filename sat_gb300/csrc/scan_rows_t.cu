@@ -15,10 +15,12 @@
 // is what keeps HBM busy with one CTA per 32 rows.  Per tile: in-thread
 // prefix, Kogge-Stone warp scan of the lane totals, plus the carry; the
 // 32-row block of results is transposed through shared memory and leaves as
-// output rows of 32 consecutive elements, one coalesced store per warp and
-// row.  The transpose buffer has rows of 32 with entry y of row x at
-// y ^ ((x / CPT) mod 32): the writes (a lane's CPT columns, fixed y) and the
-// reads (fixed x, y = lane) both touch 32 different banks.
+// output rows of 32 consecutive elements, each written as 16-byte vectors (8
+// lanes a row for 4-byte sums, 16 for 8-byte).  The transpose buffer has rows
+// of 32 entries held as 16 pairs (strip rows 2k, 2k+1: one thread's two rows)
+// with pair k of row x in slot k ^ ((x / CPT) mod 16): a warp's pair stores
+// (one slot per lane, 16 different slots per half-warp) and its 16-byte reads
+// (whole rows) both take the fewest shared-memory wavefronts.
 // Accumulators: u32 for integer outputs (mod-2^32 wrap, i32 results are the
 // two's-complement bits), f32 for f32, f64 for f64.
 #include <cuda_runtime.h>
@@ -60,8 +62,16 @@ __device__ __forceinline__ A to_acc(TIn v) {
 
 template <class TOut, class A>
 __device__ __forceinline__ TOut from_acc(A v) {
+  static_assert(sizeof(TOut) == sizeof(A), "sums are stored with their own bits");
   return (TOut)v; // u32 -> i32 keeps the bits
 }
+
+template <class A>
+__device__ __forceinline__ uint32_t bits32(A v) {
+  if constexpr (std::is_same<A, float>::value) return __float_as_uint(v);
+  else return (uint32_t)v;
+}
+__device__ __forceinline__ unsigned long long bits64(double v) { return (unsigned long long)__double_as_longlong(v); }
 
 template <class TIn>
 union Seg {
@@ -93,7 +103,7 @@ __device__ __forceinline__ void load_tile(const TIn* in, long long pitch, int W,
 template <class TIn, class TOut, class A>
 __global__ void __launch_bounds__(kWarps * 32) scan_rows_t_kernel(const TIn* __restrict__ in, long long in_pitch,
                                                                   TOut* __restrict__ out, long long out_pitch, int W,
-                                                                  int H, bool vec) {
+                                                                  int H, bool vec, bool ovec) {
   constexpr int CPT = Shape<TIn>::CPT, TW = Shape<TIn>::TW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   A* tr = reinterpret_cast<A*>(smem_raw); // TW rows of 32 (swizzled)
@@ -142,17 +152,45 @@ __global__ void __launch_bounds__(kWarps * 32) scan_rows_t_kernel(const TIn* __r
       carry[r] = carry[r] + total;
     }
     __syncthreads(); // the previous tile's transposed reads are done
-    // column x = lane CPT + c, row y = warp kRPW + r: (x / CPT) mod 32 = lane
+    // column x = lane CPT + c: the thread's two rows (2 warp, 2 warp + 1) as
+    // one pair, in pair slot warp ^ (lane mod 16) of transpose row x
 #pragma unroll
-    for (int r = 0; r < kRPW; ++r)
-#pragma unroll
-      for (int c = 0; c < CPT; ++c) tr[(lane * CPT + c) * 32 + ((warp * kRPW + r) ^ lane)] = v[r][c];
+    for (int c = 0; c < CPT; ++c) {
+      A* slot = tr + (lane * CPT + c) * 32 + 2 * (warp ^ (lane & 15));
+      if constexpr (sizeof(A) == 4) *reinterpret_cast<uint2*>(slot) = make_uint2(bits32(v[0][c]), bits32(v[1][c]));
+      else *reinterpret_cast<ulonglong2*>(slot) = make_ulonglong2(bits64(v[0][c]), bits64(v[1][c]));
+    }
     __syncthreads();
-    const int y = y0 + lane;
-#pragma unroll 4
-    for (int xr = warp; xr < TW; xr += kWarps) {
-      const int x = x0 + xr;
-      if (x < W && y < H) __stcs(out + (long long)x * out_pitch + y, from_acc<TOut, A>(tr[xr * 32 + (lane ^ ((xr / CPT) & 31))]));
+    // output rows of 32 elements as 16-byte vectors: LPR lanes a row, RPI rows
+    // a warp instruction
+    constexpr int EPV = 16 / (int)sizeof(A), LPR = 32 / EPV, RPI = 32 / LPR;
+    const int j = lane % LPR;
+#pragma unroll 2
+    for (int xr = warp * RPI + lane / LPR; xr < TW; xr += kWarps * RPI) {
+      const int h = (xr / CPT) & 15; // the swizzle of transpose row xr
+      union {
+        uint4 u;
+        A e[EPV];
+      } q;
+      if constexpr (sizeof(A) == 4) {
+        // rows 4j .. 4j+3 are pairs 2j and 2j+1: slots (2j)^h and its neighbour,
+        // one aligned 16 bytes, in swapped order when h is odd
+        q.u = *reinterpret_cast<const uint4*>(tr + xr * 32 + 4 * (j ^ (h >> 1)));
+        if (h & 1) q.u = make_uint4(q.u.z, q.u.w, q.u.x, q.u.y);
+      } else {
+        q.u = *reinterpret_cast<const uint4*>(tr + xr * 32 + 2 * (j ^ h)); // rows 2j, 2j+1
+      }
+      const int x = x0 + xr, y = y0 + j * EPV;
+      if (x < W) {
+        TOut* o = out + (long long)x * out_pitch + y;
+        if (ovec && y + EPV <= H) {
+          __stcs(reinterpret_cast<uint4*>(o), q.u); // TOut and A have the same bits
+        } else {
+#pragma unroll
+          for (int e = 0; e < EPV; ++e)
+            if (y + e < H) __stcs(o + e, from_acc<TOut, A>(q.e[e]));
+        }
+      }
     }
   }
 }
@@ -171,9 +209,10 @@ cudaError_t launch(const void* in, long long in_pitch, void* out, long long out_
     if (dev >= 0 && dev < 64) raised[dev].store(1, std::memory_order_release);
   }
   const bool vec = ((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * sizeof(TIn)) % 16 == 0;
+  const bool ovec = ((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * sizeof(TOut)) % 16 == 0;
   const unsigned grid = (unsigned)((H + kStrip - 1) / kStrip);
   scan_rows_t_kernel<TIn, TOut, A><<<grid, kWarps * 32, smem, s>>>(static_cast<const TIn*>(in), in_pitch,
-                                                                   static_cast<TOut*>(out), out_pitch, W, H, vec);
+                                                                   static_cast<TOut*>(out), out_pitch, W, H, vec, ovec);
   return cudaGetLastError();
 }
 

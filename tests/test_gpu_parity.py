@@ -508,6 +508,15 @@ def test_scan_rows_transposed_pitched_and_full_size(cuda, oracle):
     dst = empty_pitched(555, 333, 400, torch.uint32, fill=-1)
     sat_gb300.scan_rows_transposed(src, torch.uint32, out=dst)
     assert np.array_equal(to_np(dst), oracle.scan_rows(a, np.uint32).T)
+    # an output pitch of 401 elements: no 16-byte output vectors
+    dst = empty_pitched(555, 333, 401, torch.uint32, fill=-1)
+    sat_gb300.scan_rows_transposed(src, torch.uint32, out=dst)
+    assert np.array_equal(to_np(dst), oracle.scan_rows(a, np.uint32).T)
+    af = oracle.gen("f32n", 93, (333, 555))
+    dstf = empty_pitched(555, 333, 333, torch.float64)
+    sat_gb300.scan_rows_transposed(to_dev(af), torch.float64, out=dstf)
+    exact = np.cumsum(af.astype(np.float64), axis=1).T
+    assert np.abs(to_np(dstf) - exact).max() <= 1e-12 * np.abs(exact).max()
     g = torch.Generator(device=cuda).manual_seed(43)
     x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda, generator=g)
     t = sat_gb300.scan_rows_transposed(x, torch.uint32)
