@@ -195,13 +195,11 @@ Variant make_variant_rm(int in_t, int out_t, int mode, int cfg) {
 #define SG_ALL(TIN, TOUT, A, IT, OT, MODE) \
   SG_DIR(TIN, TOUT, A, IT, OT, MODE, false), SG_DIR(TIN, TOUT, A, IT, OT, MODE, true)
 
-// row-only and column-only scans (modes SG_MODE_ROWS / SG_MODE_COLS): the
-// pipelined 128-row tiles, forward
-#define SG_MODE_ROWS 2
+// column-only scans (mode SG_MODE_COLS): the pipelined 128-row tiles, forward
+// (the row-only scan has its own kernel, scan_rows_t.cu)
 #define SG_MODE_COLS 3
-#define SG_SCANS(TIN, TOUT, A, IT, OT)                                                                       \
-  satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindRows>(IT, OT, SG_MODE_ROWS, 1), \
-      satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindCols>(IT, OT, SG_MODE_COLS, 1)
+#define SG_SCANS(TIN, TOUT, A, IT, OT) \
+  satgb::make_variant<TIN, TOUT, A, false, SG_CFG1_RPW(A), 16, 1, satgb::kKindCols>(IT, OT, SG_MODE_COLS, 1)
 
 // configuration 4, for 1-byte inputs with 4-byte sums: the pipelined kernel
 // with 256-row tiles (16 warps x 16 rows) and direct stores, both directions

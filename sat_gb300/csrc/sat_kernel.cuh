@@ -644,11 +644,10 @@ struct TilePlan {
 // Maps ticket `tk` to its tile.
 // Tile orders inside a plane: anti-diagonal for the SAT (both neighbours
 // precede a tile by about a diagonal); row-major when tiles depend only on the
-// tile above (column scan), column-major when only on the tile to the left
-// (row scan) -- the orders whose concurrent tiles lie closest in memory.
+// tile above (column scan) -- the order whose concurrent tiles lie closest in
+// memory.
 constexpr int kOrderDiag = 0;
 constexpr int kOrderRows = 1;
-constexpr int kOrderCols = 2;
 
 template <bool REV, int ORDER = kOrderDiag>
 __device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long long tk) {
@@ -686,9 +685,6 @@ __device__ __noinline__ TilePlan plan_tile(const SatParams& P, unsigned long lon
   if (ORDER == kOrderRows) {
     ty = (int)(li / ntx);
     tx = (int)(li - (long long)ty * ntx);
-  } else if (ORDER == kOrderCols) {
-    tx = (int)(li / nty);
-    ty = (int)(li - (long long)tx * nty);
   } else {
     diag_tile(li, ntx, nty, tx, ty);
   }
@@ -767,12 +763,12 @@ __device__ __noinline__ bool produce(const SatParams& P, unsigned long long tk, 
 //
 // The reverse (suffix) SAT runs every scan in the opposite direction.
 // ---------------------------------------------------------------------------
-// What the tile kernel computes: the SAT, or only its row scan (each row's
-// prefix sums: the reference's ScanX, IncrementScanX.cu:12-113) or only its
-// column scan (ScanY, IncrementScanY.cu:10-126).  The single-direction scans
-// keep one look-back (rows or columns) and no corner.
+// What the tile kernel computes: the SAT, or only its column scan (each
+// column's prefix sums: the reference's ScanY, IncrementScanY.cu:10-126),
+// which keeps the column look-back and no corner.  The row-only scan (ScanX,
+// IncrementScanX.cu:12-113) needs no look-back and has its own kernel
+// (scan_rows_t.cu).
 constexpr int kKindSat = 0;
-constexpr int kKindRows = 1;
 constexpr int kKindCols = 2;
 
 template <class TIn, class TOut, class A, bool REV, int RPW, int NW, int MINB, int KIND = kKindSat,
@@ -798,7 +794,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
   constexpr int CH = RP;             // ... and values per lane
   constexpr int K = Ar<A>::K;
   constexpr bool WIDEN = !DIRECT && sizeof(TIn) < sizeof(TOut); // outputs overlap other threads' inputs in the stage
-  constexpr int ORDER = KIND == kKindCols ? kOrderRows : KIND == kKindRows ? kOrderCols : kOrderDiag;
+  constexpr int ORDER = KIND == kKindCols ? kOrderRows : kOrderDiag;
   using AR = Ar<A>;
 
   extern __shared__ __align__(128) unsigned char dsmem[];
@@ -953,7 +949,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       A ac = AR::zero();
 #pragma unroll
       for (int w = 0; w < NW; ++w) ac = AR::add(ac, s_colp[kk & 1][w][j]);
-      if (KIND != kKindRows && (REV ? (nxt.ty > 0) : (nxt.ty < nty - 1)) && !stall)
+      if ((REV ? (nxt.ty > 0) : (nxt.ty < nty - 1)) && !stall)
         publish<A>(P.col_words + ((unsigned long long)t * TW + j) * K, ac, tagA);
       A run = AR::zero();
 #pragma unroll
@@ -996,7 +992,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
       my_agg = agg_cur;
       // the current tile's first column / corner look-back window: read now,
       // used after A(k+1), so the round trip overlaps the local phase
-      if ((KIND != kKindRows && tid < TW) || (KIND == kKindSat && warp == CW && lane == 0))
+      if ((tid < TW) || (KIND == kKindSat && warp == CW && lane == 0))
         early_read<A>(my_win, my_base, my_stride, my_steps);
     }
     // Row threads run the row look-back of the NEXT tile (k+1) in this
@@ -1037,7 +1033,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
     A got = AR::zero();
     const bool lb_row = tid >= TW && tid < TW + TH && rt >= 0;
     const bool lb_cur =
-        has_cur && ((KIND != kKindRows && tid < TW) || (KIND == kKindSat && warp == CW && lane == 0));
+        has_cur && ((tid < TW) || (KIND == kKindSat && warp == CW && lane == 0));
     if (lb_row || lb_cur) {
       const long long stride = lb_row ? (REV ? 1 : -1) * (long long)TH * K : my_stride;
       const int steps = lb_row ? (REV ? (rntx - 1 - rtx) : rtx) : my_steps;
@@ -1048,7 +1044,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
         // nothing to do for the columns before the first tile
       } else {
         const A above = got;
-        if (KIND != kKindRows && pub_col && !stall)
+        if (pub_col && !stall)
           publish<A>(P.col_words + ((unsigned long long)t * TW + tid) * K, AR::add(above, my_agg), tagI);
         s_colabove[tid] = above;
       }
@@ -1191,7 +1187,7 @@ __global__ void __launch_bounds__(NW * 32, MINB) sat_tile_kernel(const __grid_co
           } else {
             run = AR::add(run, a);
             if (KIND == kKindSat) top[c] = AR::add(top[c], run);
-            o.e[c] = OutCvt<TOut, A>::out(KIND == kKindRows ? run : top[c]);
+            o.e[c] = OutCvt<TOut, A>::out(top[c]);
           }
         }
         if (DIRECT) {

@@ -561,6 +561,13 @@ satgb_status launch_locked(const Variant* v, const ImageDesc* table_dev, const I
 
 // internal modes of the variant table: the row-only and column-only scans
 constexpr int kModeRows = 2;
+}  // namespace
+namespace satgb {
+satgb_status scan_rows_strips(int in_t, int out_t, const void* d_in, int64_t in_pitch, int64_t in_plane, void* d_out,
+                              int64_t out_pitch, int64_t out_plane, int64_t width, int64_t height, int64_t planes,
+                              cudaStream_t s);
+}  // namespace satgb
+namespace {
 constexpr int kModeCols = 3;
 
 satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in, long long in_pitch,
@@ -572,7 +579,8 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
   if (mode != SATGB_MODE_PLAIN && mode != SATGB_MODE_COMPENSATED && mode != kModeRows && mode != kModeCols)
     return fail(SATGB_ERR_INVALID_ARG, "unknown mode %d", mode);
   if (dir != SATGB_FORWARD && dir != SATGB_REVERSE) return fail(SATGB_ERR_INVALID_ARG, "unknown direction %d", dir);
-  if (!pair_offered(in_t, out_t, mode))
+  // the row-only scan (its own kernel) offers the plain SAT's pairs
+  if (!pair_offered(in_t, out_t, mode == kModeRows ? (int)SATGB_MODE_PLAIN : mode))
     return fail(SATGB_ERR_UNSUPPORTED_TYPES, "type pair %s -> %s%s not offered", dtype_name(in_t), dtype_name(out_t),
                 mode == SATGB_MODE_COMPENSATED ? " (compensated)" : "");
   if (planes < 0) return fail(SATGB_ERR_INVALID_ARG, "negative plane count");
@@ -595,6 +603,11 @@ satgb_status sat_single(int in_t, int out_t, int mode, int dir, const void* d_in
     const bool same = ib == ob && in_sz == out_sz && in_pitch == out_pitch && in_plane == out_plane;
     if (!same && ib < oe && ob < ie) return fail(SATGB_ERR_INVALID_ARG, "input and output stacks overlap");
   }
+
+  // the row-only scan has no look-back: its own kernel (scan_rows_t.cu), no workspace
+  if (mode == kModeRows && dir == SATGB_FORWARD)
+    return scan_rows_strips(in_t, out_t, d_in, in_pitch, planes > 1 ? in_plane : 0, d_out, out_pitch,
+                            planes > 1 ? out_plane : 0, width, height, planes, s);
 
   std::lock_guard<std::mutex> lk(g_mu);
   int dev = 0;

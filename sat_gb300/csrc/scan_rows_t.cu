@@ -216,6 +216,99 @@ cudaError_t launch(const void* in, long long in_pitch, void* out, long long out_
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Row scan, untransposed (satgb_scan_rows): out(y, x) = sum_{i <= x} in(y, i)
+// in the input's own layout.  Rows are independent and the output needs no
+// transpose, so every warp works alone: it owns two rows, walks them left to
+// right in the same tiles as above (one 16-byte input vector per lane and
+// row, two tiles in flight, the running sums in registers) and stores each
+// lane's CPT results of a row straight from registers as 16-byte vectors.
+// No shared memory, no barrier; CTAs of 4 warps, so that the rows spread over
+// every SM.
+constexpr int kRowWarps = 4;
+
+template <class TIn, class TOut, class A>
+__global__ void __launch_bounds__(kRowWarps * 32) scan_rows_strip_kernel(const TIn* __restrict__ in, long long in_pitch,
+                                                                         long long in_plane, TOut* __restrict__ out,
+                                                                         long long out_pitch, long long out_plane, int W,
+                                                                         int H, bool vec, bool ovec) {
+  constexpr int CPT = Shape<TIn>::CPT, TW = Shape<TIn>::TW;
+  constexpr int OV = CPT * (int)sizeof(TOut) / 16; // 16-byte output vectors per lane and row
+  static_assert(CPT * sizeof(TOut) % 16 == 0, "whole output vectors");
+  const int lane = threadIdx.x & 31;
+  const int yw = (blockIdx.x * kRowWarps + (threadIdx.x >> 5)) * kRPW;
+  if (yw >= H) return;
+  in += blockIdx.y * in_plane;
+  out += blockIdx.y * out_plane;
+  A carry[kRPW];
+#pragma unroll
+  for (int r = 0; r < kRPW; ++r) carry[r] = A(0);
+  uint4 n0[kRPW], n1[kRPW];
+  load_tile<TIn>(in, in_pitch, W, H, yw, lane * CPT, vec, n0);
+  if (TW < W) load_tile<TIn>(in, in_pitch, W, H, yw, TW + lane * CPT, vec, n1);
+  for (int x0 = 0; x0 < W; x0 += TW) {
+    Seg<TIn> cur[kRPW];
+#pragma unroll
+    for (int r = 0; r < kRPW; ++r) {
+      cur[r].u = n0[r];
+      n0[r] = n1[r];
+    }
+    if (x0 + 2 * TW < W) load_tile<TIn>(in, in_pitch, W, H, yw, x0 + 2 * TW + lane * CPT, vec, n1);
+    const int x = x0 + lane * CPT;
+#pragma unroll
+    for (int r = 0; r < kRPW; ++r) {
+      union {
+        uint4 u[OV];
+        TOut e[CPT];
+      } o;
+      A v = A(0); // the lane's total
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) v = v + to_acc<A>(cur[r].e[c]);
+      A incl = v;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const A t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl = t + incl;
+      }
+      A ex = __shfl_up_sync(0xffffffffu, incl, 1);
+      if (lane == 0) ex = A(0);
+      const A base = carry[r] + ex;
+      carry[r] = carry[r] + __shfl_sync(0xffffffffu, incl, 31);
+      A run = base;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        run = run + to_acc<A>(cur[r].e[c]);
+        o.e[c] = from_acc<TOut, A>(run);
+      }
+      const int y = yw + r;
+      if (y < H && x < W) {
+        TOut* orow = out + (long long)y * out_pitch + x;
+        if (ovec && x + CPT <= W) {
+#pragma unroll
+          for (int q = 0; q < OV; ++q) __stcs(reinterpret_cast<uint4*>(orow) + q, o.u[q]);
+        } else {
+#pragma unroll
+          for (int c = 0; c < CPT; ++c)
+            if (x + c < W) __stcs(orow + c, o.e[c]);
+        }
+      }
+    }
+  }
+}
+
+template <class TIn, class TOut, class A>
+cudaError_t launch_rows(const void* in, long long in_pitch, long long in_plane, void* out, long long out_pitch,
+                        long long out_plane, int W, int H, int planes, cudaStream_t s) {
+  const bool vec = ((uintptr_t)in % 16) == 0 && ((size_t)in_pitch * sizeof(TIn)) % 16 == 0 &&
+                   (planes == 1 || ((size_t)in_plane * sizeof(TIn)) % 16 == 0);
+  const bool ovec = ((uintptr_t)out % 16) == 0 && ((size_t)out_pitch * sizeof(TOut)) % 16 == 0 &&
+                    (planes == 1 || ((size_t)out_plane * sizeof(TOut)) % 16 == 0);
+  const dim3 grid((unsigned)((H + kRowWarps * kRPW - 1) / (kRowWarps * kRPW)), (unsigned)planes);
+  scan_rows_strip_kernel<TIn, TOut, A><<<grid, kRowWarps * 32, 0, s>>>(
+      static_cast<const TIn*>(in), in_pitch, in_plane, static_cast<TOut*>(out), out_pitch, out_plane, W, H, vec, ovec);
+  return cudaGetLastError();
+}
+
 size_t elem_size(int t) {
   switch (t) {
     case SATGB_U8:
@@ -277,3 +370,35 @@ extern "C" satgb_status satgb_scan_rows_transposed(satgb_dtype in_t, satgb_dtype
   satgb::api_count_launch();
   return SATGB_OK;
 }
+
+namespace satgb {
+// satgb_scan_rows' kernel, for arguments the caller has validated (sizes,
+// pitches, overlap, type pair): planes of width x height at the given strides.
+satgb_status scan_rows_strips(int in_t, int out_t, const void* d_in, int64_t in_pitch, int64_t in_plane, void* d_out,
+                              int64_t out_pitch, int64_t out_plane, int64_t width, int64_t height, int64_t planes,
+                              cudaStream_t s) {
+  if (width > (1LL << 31) - 3 * kMaxTileW || height > (1LL << 31) - 2 * kStrip || planes > 65535)
+    return api_fail(SATGB_ERR_OVERFLOW, "scan_rows: image too large");
+  const int W = (int)width, H = (int)height, NP = (int)planes;
+  cudaError_t e = cudaSuccess;
+#define SG_R(IT, OT, TIN, TOUT, A) \
+  if (in_t == IT && out_t == OT) e = launch_rows<TIN, TOUT, A>(d_in, in_pitch, in_plane, d_out, out_pitch, out_plane, W, H, NP, s); else
+  SG_R(SATGB_U8, SATGB_U32, uint8_t, uint32_t, uint32_t)
+  SG_R(SATGB_U8, SATGB_F32, uint8_t, float, float)
+  SG_R(SATGB_U8, SATGB_F64, uint8_t, double, double)
+  SG_R(SATGB_I8, SATGB_I32, int8_t, int32_t, uint32_t)
+  SG_R(SATGB_I8, SATGB_F32, int8_t, float, float)
+  SG_R(SATGB_I8, SATGB_F64, int8_t, double, double)
+  SG_R(SATGB_I32, SATGB_I32, int32_t, int32_t, uint32_t)
+  SG_R(SATGB_I32, SATGB_F64, int32_t, double, double)
+  SG_R(SATGB_U32, SATGB_U32, uint32_t, uint32_t, uint32_t)
+  SG_R(SATGB_F32, SATGB_F32, float, float, float)
+  SG_R(SATGB_F32, SATGB_F64, float, double, double)
+  SG_R(SATGB_F64, SATGB_F64, double, double, double)
+  return api_fail(SATGB_ERR_UNSUPPORTED_TYPES, "scan_rows: type pair not offered");
+#undef SG_R
+  if (e != cudaSuccess) return api_cuda_fail(e, "scan_rows_strip_kernel launch");
+  api_count_launch();
+  return SATGB_OK;
+}
+}  // namespace satgb

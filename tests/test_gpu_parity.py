@@ -468,7 +468,7 @@ def test_row_and_column_scans_all_pairs(cuda, oracle, which):
     ref = oracle.scan_rows if which == "rows" else oracle.scan_cols
     axis = 1 if which == "rows" else 0
     for name, (ti, to) in oracle.PAIRS.items():
-        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (129, 257), (517, 769)]):
+        for i, shape in enumerate([(1, 1), (3, 700), (700, 3), (129, 257), (517, 769), (37, 1601)]):
             a = oracle.gen(PAIR_KINDS[ti], 3000 + i, shape)
             out = to_np(fn(to_dev(a), SCAN_TORCH[np.dtype(to)]))
             if np.dtype(to).kind in "iu":
@@ -556,9 +556,17 @@ def test_scans_pitched_and_full_size(cuda, oracle):
     src = empty_pitched(333, 555, 640, torch.uint8)
     src.copy_(to_dev(a))
     for fn, ref in ((sat_gb300.scan_rows, oracle.scan_rows), (sat_gb300.scan_cols, oracle.scan_cols)):
-        dst = empty_pitched(333, 555, 600, torch.uint32, fill=-1)
-        fn(src, torch.uint32, out=dst)
-        assert np.array_equal(to_np(dst), ref(a, np.uint32))
+        for opitch in (600, 601):  # 601: no 16-byte output vectors
+            dst = empty_pitched(333, 555, opitch, torch.uint32, fill=-1)
+            fn(src, torch.uint32, out=dst)
+            assert np.array_equal(to_np(dst), ref(a, np.uint32))
+    # in place (f32 -> f32 into its own buffer)
+    af = oracle.gen("f32n", 94, (300, 1000))
+    y = to_dev(af)
+    sat_gb300.scan_rows(y, torch.float32, out=y)
+    exact = np.cumsum(af.astype(np.float64), axis=1)
+    den = np.cumsum(np.abs(af.astype(np.float64)), axis=1)
+    assert (np.abs(to_np(y).astype(np.float64) - exact) / np.maximum(den, 1e-300)).max() <= TOL[np.dtype(np.float32)]
     x = torch.randint(0, 256, (8192, 8192), dtype=torch.uint8, device=cuda)
     r = sat_gb300.scan_rows(x, torch.uint32)
     c = sat_gb300.scan_cols(x, torch.uint32)
