@@ -1,8 +1,10 @@
-// scan_rows_t.cu -- row scan with transposed output:
+// scan_rows_t.cu -- the row scans, which need no look-back: the row scan with
+// transposed output (satgb_scan_rows_transposed) and, further down, the plain
+// row scan (satgb_scan_rows).
 //
-//   out(x, y) = sum_{i <= x} in(y, i)      in: W x H (row y, column x), out: H x W
+//   transposed: out(x, y) = sum_{i <= x} in(y, i)   in: W x H (row y, column x), out: H x W
 //
-// the reference's SerielScan::TestX (integralImage/BRLT-Scan.cu:128-190), whose
+// is the reference's SerielScan::TestX (integralImage/BRLT-Scan.cu:128-190), whose
 // serielScan launch reads rows and stores the scanned rows transposed
 // (compared there with IntegralImageAllRow + Transpose).  Rows are
 // independent, so there is no look-back: a CTA owns a strip of 32 rows and
