@@ -81,6 +81,26 @@ def test_scan_rows_transposed_validation(satlib):
     assert call(h=0, d_in=0, d_out=0) == _lib.OK
 
 
+def test_scan_rows_validation(satlib):
+    """The row-only scan (its own kernel, no workspace) validates like the
+    SAT entry points and offers the same pairs; sizes beyond its kernel's
+    32-bit column and row indices are refused before any launch."""
+    f = satlib.satgb_scan_rows
+    U8, U32 = _lib.U8, _lib.U32
+
+    def call(in_t=U8, out_t=U32, d_in=0x1000, ip=16, d_out=0x10000000000, op=16, w=16, h=8):
+        return f(in_t, out_t, d_in, ip, d_out, op, w, h, None)
+
+    assert call(w=-1) == _lib.ERR_INVALID_ARG
+    assert call(d_out=0) == _lib.ERR_INVALID_ARG
+    assert call(ip=15) == _lib.ERR_INVALID_ARG
+    assert call(in_t=_lib.U16) == _lib.ERR_UNSUPPORTED_TYPES
+    assert call(in_t=_lib.F32, out_t=U32) == _lib.ERR_UNSUPPORTED_TYPES
+    assert call(w=(1 << 31) - 16, ip=1 << 31, op=1 << 31, h=1) == _lib.ERR_OVERFLOW
+    assert call(w=0) == _lib.OK
+    assert call(h=0, d_in=0, d_out=0) == _lib.OK
+
+
 def test_box_filter_validation(satlib):
     """Box-filter descriptors are checked before any launch: radii count and
     sign, sizes within the launch grid (height up to 65535 x 32), plane count,
