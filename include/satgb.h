@@ -232,6 +232,11 @@ satgb_status satgb_sat_noalloc(const satgb_sat_desc* desc, satgb_stream stream);
 /* classes' launches, one after the other, in one CUDA graph; exec replays    */
 /* the graph on `stream`.  All images share one dtype pair, mode and          */
 /* direction.  No image may write memory another image reads or writes.       */
+/* Inputs whose rows TMA cannot address (base or row pitch not a multiple of  */
+/* 16 bytes, rows of at least 16 bytes: e.g. packed u8 rows of odd widths)    */
+/* are copied by each exec, as the graph's first launch, into rows padded to  */
+/* 16 bytes in a staging buffer the plan allocates (about the size of those   */
+/* inputs, through the allocator hooks when set) and frees on destroy.        */
 /* ------------------------------------------------------------------------- */
 typedef struct {
   const void* d_in;

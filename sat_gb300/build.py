@@ -30,6 +30,7 @@ SOURCES = [
     "box_filter.cu",
     "scan_rows_t.cu",
     "satgb_noalloc.cu",
+    "batch_repack.cu",
 ]
 
 

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/satgb.h"
+#include "batch_repack.h"
 #include "sat_kernel.cuh"
 #include "sat_registry.h"
 
@@ -674,6 +675,12 @@ struct satgb_batch_plan_s {
   int in_t = 0, out_t = 0, mode = 0, dir = 0;
   int dev = 0;
   bool all_tma = true; // every image's rows can go through TMA (16-byte aligned bases and pitches)
+  // Inputs whose rows TMA cannot address are copied at each execution into
+  // padded rows of `stage` (batch_repack.cu); `jobs` (device) lists them.
+  void* stage = nullptr;
+  satgb::RepackJob* jobs = nullptr;
+  int n_jobs = 0;
+  long long stage_rows = 0;
   BatchSeg seg[kBatchClasses];
   long long n_tiles = 0;
   Workspace ws;
@@ -1049,7 +1056,13 @@ satgb_status plan_ws(satgb_batch_plan_s* p, cudaStream_t s) {
   return e == cudaSuccess ? SATGB_OK : cuda_fail(e, "cudaStreamSynchronize");
 }
 
+satgb_status plan_repack(satgb_batch_plan_s* p, cudaStream_t s) {
+  return repack_launch(p->jobs, p->n_jobs, p->stage_rows, sms_of(p->dev), s);
+}
+
 satgb_status plan_launch_locked(satgb_batch_plan_s* p, cudaStream_t s) {
+  satgb_status st0 = plan_repack(p, s);
+  if (st0 != SATGB_OK) return st0;
   for (auto& g : p->seg) {
     if (!g.n_tiles) continue;
     satgb_status st = launch_locked(g.v, g.table, g.img0, g.n_images, g.n_tiles, p->ws, p->dev, s, g.order);
@@ -1090,8 +1103,60 @@ void plan_free(satgb_batch_plan_s* p) {
   if (p->exec) cudaGraphExecDestroy(p->exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   ws_free(p->ws.base);
+  ws_free(p->stage);
+  if (p->jobs) cudaFree(p->jobs);
   for (auto& g : p->seg) seg_free(g);
   delete p;
+}
+
+// Inputs that TMA cannot address (base or row pitch not 16-byte aligned, at
+// least 16 bytes a row) get a copy in padded rows: the plan's staging buffer,
+// one region per image (256-byte aligned, rows of the width rounded up to 16
+// bytes), and the tile kernels read the copies.  Rewrites the images' input
+// pointers and pitches in `imgs`.
+satgb_status plan_stage_inputs(satgb_batch_plan_s* p, std::vector<ImgCheck>& imgs, size_t in_sz, cudaStream_t s) {
+  std::vector<satgb::RepackJob> jobs;
+  std::vector<size_t> offs, which;
+  size_t total = 0;
+  long long rows = 0;
+  for (size_t i = 0; i < imgs.size(); ++i) {
+    const ImgCheck& c = imgs[i];
+    const size_t row_bytes = (size_t)c.width * in_sz;
+    if (row_bytes < 16 || tma_ok(c.in, c.width, c.height, c.in_pitch, 1, 0, in_sz)) continue;
+    const size_t pitch = (row_bytes + 15) & ~(size_t)15;
+    satgb::RepackJob j;
+    j.src = static_cast<const unsigned char*>(c.in);
+    j.dst = nullptr;
+    j.src_pitch = c.in_pitch * (int64_t)in_sz;
+    j.dst_pitch = (int64_t)pitch;
+    j.row_bytes = (int64_t)row_bytes;
+    j.row_base = rows;
+    jobs.push_back(j);
+    which.push_back(i);
+    offs.push_back(total);
+    total += ((pitch * (size_t)c.height) + 255) & ~(size_t)255;
+    rows += c.height;
+  }
+  if (jobs.empty()) return SATGB_OK;
+  p->stage = ws_alloc(total);
+  if (!p->stage) return fail(SATGB_ERR_ALLOC, "batch staging allocation of %zu bytes failed", total);
+  for (size_t k = 0; k < jobs.size(); ++k) {
+    ImgCheck& c = imgs[which[k]];
+    jobs[k].dst = static_cast<unsigned char*>(p->stage) + offs[k];
+    c.in = jobs[k].dst;
+    c.in_pitch = jobs[k].dst_pitch / (int64_t)in_sz;
+  }
+  if (cudaMalloc(&p->jobs, jobs.size() * sizeof(satgb::RepackJob)) != cudaSuccess) {
+    cudaGetLastError();
+    p->jobs = nullptr;
+    return fail(SATGB_ERR_ALLOC, "batch staging table allocation failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(p->jobs, jobs.data(), jobs.size() * sizeof(satgb::RepackJob), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "batch staging table upload");
+  p->n_jobs = (int)jobs.size();
+  p->stage_rows = rows;
+  return SATGB_OK;
 }
 
 }  // namespace
@@ -1132,6 +1197,11 @@ satgb_status satgb_batch_plan_create(satgb_batch_plan** plan, satgb_dtype in_t, 
   p->mode = mode;
   p->dir = direction;
   p->dev = dev;
+  st = plan_stage_inputs(p, keep, in_sz, s);
+  if (st != SATGB_OK) {
+    plan_free(p);
+    return st;
+  }
   const int cpt = (int)(16 / out_sz);
   for (auto& c : keep) {
     const long long tiles = ((c.width + 32LL * cpt - 1) / (32LL * cpt)) * ((c.height + 127) / 128);
@@ -1172,7 +1242,7 @@ satgb_status satgb_batch_plan_autotune(satgb_batch_plan* p, satgb_stream stream,
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return cuda_fail(cudaGetLastError(), "cudaEventCreate");
-  satgb_status st = SATGB_OK;
+  satgb_status st = plan_repack(p, s); // the staged inputs the timed launches read
   for (int cls = 0; cls < kBatchClasses && st == SATGB_OK; ++cls) {
     BatchSeg& g = p->seg[cls];
     if (configs) configs[cls] = -1;

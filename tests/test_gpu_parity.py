@@ -274,6 +274,36 @@ def test_batch_plan_uneven(cuda, oracle):
     plan.close()
 
 
+def test_batch_plan_stages_unaligned_inputs_each_exec(cuda, oracle):
+    """Inputs whose rows TMA cannot address (packed rows of odd widths, an
+    offset base) are copied into the plan's padded staging rows at every
+    execution: after the caller changes its inputs in place, the next exec
+    reads the new values.  Mixed with 16-byte pitched images and rows shorter
+    than 16 bytes, which are not staged."""
+    rng = np.random.default_rng(9)
+    ins, outs, views = [], [], []
+    for i in range(24):
+        h, w = int(rng.integers(1, 400)), int(rng.integers(1, 900))
+        if i % 3 == 0:  # 16-byte pitched rows: TMA reads them in place
+            x = empty_pitched(h, w, (w + 15) // 16 * 16, torch.uint8)
+        elif i % 3 == 1:  # packed rows, one byte past a 16-byte boundary
+            x = torch.empty(h * w + 1, dtype=torch.uint8, device=cuda)[1:].view(h, w)
+        else:  # packed rows
+            x = torch.empty((h, w), dtype=torch.uint8, device=cuda)
+        ins.append(x)
+        outs.append(torch.empty((h, w), dtype=torch.uint32, device=cuda))
+    plan = sat_gb300.BatchPlan(ins, outs)
+    for rep in range(2):
+        arrs = [oracle.gen("u8", 6000 + 100 * rep + i, tuple(x.shape)) for i, x in enumerate(ins)]
+        for x, a in zip(ins, arrs):
+            x.copy_(to_dev(a))
+        plan.exec()
+        plan.check()
+        for a, o in zip(arrs, outs):
+            assert np.array_equal(to_np(o), oracle.sat_serial(a, np.uint32)), rep
+    plan.close()
+
+
 def test_batch_plan_float_and_reverse(cuda, oracle):
     rng = np.random.default_rng(6)
     ins, outs, arrs = [], [], []
