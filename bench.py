@@ -446,6 +446,9 @@ CASES = {
     "f32c_16384": ("float32", "float32", "compensated", False, 16384, 16384),
     "f32t_8192": ("float32", "float32", "rows_transposed", False, 8192, 8192),
     "u8t_8192": ("uint8", "uint32", "rows_transposed", False, 8192, 8192),
+    "f32rows_8192": ("float32", "float32", "rows", False, 8192, 8192),
+    "u8rows_8192": ("uint8", "uint32", "rows", False, 8192, 8192),
+    "f32cols_8192": ("float32", "float32", "cols", False, 8192, 8192),
 }
 
 
@@ -473,6 +476,9 @@ def run_case(args):
     if mode == "rows_transposed":
         y = y.t().contiguous() if h != w else y
         fn = lambda: sat_gb300.scan_rows_transposed(x, tout, out=y)
+    elif mode in ("rows", "cols"):
+        scan = sat_gb300.scan_rows if mode == "rows" else sat_gb300.scan_cols
+        fn = lambda: scan(x, tout, out=y)
     else:
         fn = lambda: sat_gb300.sat(x, tout, mode=mode, reverse=rev, out=y)
     total, per = _time_steps(fn, args.steps, args.warmup, stream, 0.0)
