@@ -37,8 +37,11 @@
  *
  * Scratch: the look-back status words live in a per-stream workspace that the
  * library allocates on first use (and grows when a larger image arrives) and
- * frees in satgb_release().  Calls on distinct streams may run concurrently;
- * calls on one stream are ordered by the stream.
+ * frees in satgb_release().  A call on an image of 1-byte inputs of at least
+ * 2^22 pixels whose rows are not 16-byte aligned (base or pitch) also copies
+ * its input into padded rows in that workspace (one extra launch; the
+ * workspace grows by about the input's size).  Calls on distinct streams may
+ * run concurrently; calls on one stream are ordered by the stream.
  */
 #ifndef SATGB_H
 #define SATGB_H

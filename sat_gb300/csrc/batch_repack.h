@@ -20,5 +20,7 @@ struct RepackJob {
 // One launch for every staged row of n_jobs images (jobs sorted by row_base,
 // in device memory), on up to 8 CTAs of 8 warps per SM.
 satgb_status repack_launch(const RepackJob* jobs_dev, int n_jobs, long long n_rows, int sms, cudaStream_t s);
+// One image's n_rows rows (row_base 0), the job passed by value.
+satgb_status repack_launch_one(const RepackJob& job, long long n_rows, int sms, cudaStream_t s);
 
 }  // namespace satgb

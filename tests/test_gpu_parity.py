@@ -304,6 +304,30 @@ def test_batch_plan_stages_unaligned_inputs_each_exec(cuda, oracle):
     plan.close()
 
 
+@pytest.mark.parametrize("layout", ["packed", "offset"])
+def test_single_image_staged_input(cuda, oracle, layout):
+    """A single image of 1-byte inputs, at least 2^22 pixels, whose rows TMA
+    cannot address (packed rows of an odd width, or a base one byte past a
+    16-byte boundary) is copied into padded rows of the workspace by one more
+    launch before the tile kernel: bit-exact against the oracle, both
+    directions, and again after the input changes in place."""
+    h, w = 2049, 2051
+    n = h * w + 1
+    for rev in (False, True):
+        for rep in range(2):
+            a = oracle.gen("u8", 7100 + 10 * rep + rev, (h, w))
+            if layout == "packed":
+                x = to_dev(a)
+            else:
+                x = torch.empty(n + 16, dtype=torch.uint8, device=cuda)[1:1 + h * w].view(h, w)
+                x.copy_(to_dev(a))
+            before = sat_gb300.launch_count()
+            out = sat_gb300.sat(x, torch.uint32, reverse=rev)
+            assert sat_gb300.launch_count() - before == 2  # the staging copy and the SAT
+            ref = oracle.sat_reverse(a, np.uint32) if rev else oracle.sat_serial(a, np.uint32)
+            assert np.array_equal(to_np(out), ref), (layout, rev, rep)
+
+
 def test_batch_plan_float_and_reverse(cuda, oracle):
     rng = np.random.default_rng(6)
     ins, outs, arrs = [], [], []
