@@ -310,7 +310,9 @@ const char* satgb_last_error_string(void);
 satgb_status satgb_release(void);
 
 /* Pre-sizes the workspace of `stream` for images up to width x height, so that
- * a later call does not allocate (e.g. inside CUDA stream capture). */
+ * a later call does not allocate (e.g. inside CUDA stream capture); this
+ * includes the staging rows a large image of 1-byte inputs with unaligned
+ * rows needs. */
 satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream);
 
 /* Allocation hook for the workspace (NULL restores cudaMalloc/cudaFree). */

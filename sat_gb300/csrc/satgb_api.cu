@@ -833,8 +833,10 @@ satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream) {
   int dev = 0;
   satgb_status st = get_device(&dev);
   if (st != SATGB_OK) return st;
-  // the largest layout over every variant
+  // the largest layout over every variant, with the staging rows of a 1-byte
+  // input behind it where a call would stage one (sat_single)
   size_t need = 0;
+  const size_t stage = width * height >= kStageMinPixels ? (((size_t)width + 15) & ~(size_t)15) * (size_t)height : 0;
   using ListFn = const Variant* (*)(int*);
   static const ListFn lists[] = {variants_u8, variants_i8, variants_int32, variants_f32, variants_f64};
   for (ListFn f : lists) {
@@ -842,7 +844,8 @@ satgb_status satgb_reserve(int64_t width, int64_t height, satgb_stream stream) {
     const Variant* v = f(&n);
     for (int i = 0; i < n; ++i) {
       long long nt = ((width + v[i].TW - 1) / v[i].TW) * ((height + v[i].TH - 1) / v[i].TH);
-      need = std::max(need, layout_for(nt, &v[i]).total);
+      const size_t look = layout_for(nt, &v[i]).total;
+      need = std::max(need, dtype_size(v[i].in_t) == 1 && stage ? ((look + 255) & ~(size_t)255) + stage : look);
     }
   }
   Workspace& ws = g_ws[std::make_pair(dev, (void*)stream)];
