@@ -328,6 +328,29 @@ def test_single_image_staged_input(cuda, oracle, layout):
             assert np.array_equal(to_np(out), ref), (layout, rev, rep)
 
 
+def test_reserve_then_capture_staged_call(cuda, oracle):
+    """satgb_reserve sizes the stream's workspace for the staging rows too: a
+    staged single-image call (packed u8 rows, 2049 x 2051) can then be captured
+    in a CUDA graph, which allows no allocation, and the replay is bit-exact."""
+    h, w = 2049, 2051
+    a = oracle.gen("u8", 7300, (h, w))
+    x = to_dev(a)
+    y = torch.empty((h, w), dtype=torch.int32, device=cuda).view(torch.uint32)
+    s = torch.cuda.Stream()
+    L = _lib.load()
+    with torch.cuda.stream(s):
+        assert L.satgb_reserve(w, h, s.cuda_stream) == _lib.OK
+        sat_gb300.sat(x, torch.uint32, out=y)  # descriptors encoded before the capture
+        s.synchronize()
+        y.zero_()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            sat_gb300.sat(x, torch.uint32, out=y)
+        g.replay()
+        s.synchronize()
+    assert np.array_equal(to_np(y), oracle.sat_serial(a, np.uint32))
+
+
 def test_batch_plan_float_and_reverse(cuda, oracle):
     rng = np.random.default_rng(6)
     ins, outs, arrs = [], [], []
