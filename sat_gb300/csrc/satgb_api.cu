@@ -516,12 +516,19 @@ int default_config(long long width, long long height, int sms, int in_sz, int ou
   sms = std::max(1, sms);
   if (out_sz == 8) return tiles128 >= 8LL * sms ? 0 : 2;
   if (compensated) return tiles128 >= sms ? 3 : 2;
+  // Small single images: the row-major kernel (configuration 6), whose short
+  // tile rows make its sums over the row aggregates cheap (f32 1536^2 17.8 ->
+  // 14.9 us, 2048^2 21.2 -> 19.1, 3072^2 29.3 -> 27.7; u8 -> u32 1024^2 15.2 ->
+  // 12.9); stacks of small planes stay on configuration 1.
+  const bool single = planes <= 1;
   if (in_sz == 1) {
     if (plane_tiles >= 16LL * sms) return 5;
+    if (single && plane_tiles < 3LL * sms) return 6;
     if (ntx * ((height + 255) / 256) * std::max(1LL, planes) >= 64) return 4;
-    return 1;
+    return single ? 6 : 1;
   }
-  return plane_tiles >= 4LL * sms ? 5 : 1;
+  if (plane_tiles >= 4LL * sms) return 5;
+  return single ? 6 : 1;
 }
 
 int choose_config_locked(int in_t, int out_t, int mode, int dir, long long w, long long h, int dev,
